@@ -1,0 +1,148 @@
+/*
+ * gspec.h - C ABI of the GB300-native EDD gated spectrometer.
+ *
+ * Drop-in boundary for psrdada_cpp's GatedSpectrometer handler
+ * (psrdada_cpp/effelsberg/edd/GatedSpectrometer.cuh:270-366).  Plain
+ * pointers, sizes and status codes only; no C++ types or exceptions cross
+ * this boundary.  The C++ template include/psrdada_cpp_gb300/GatedSpectrometer.hpp
+ * and the Python module psrdada_cpp_gb300.gated_spectrometer wrap it with the
+ * reference's init(RawBytes&) / operator()(RawBytes&) interface.
+ *
+ * Status codes: GSPEC_OK (0), GSPEC_STOP (1, the block size did not match:
+ * the reference's operator() returns true), negative values are errors whose
+ * text gspec_last_error() returns.
+ */
+#ifndef GSPEC_H
+#define GSPEC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GSPEC_OK 0
+#define GSPEC_STOP 1
+#define GSPEC_ERR_ARG (-1)
+#define GSPEC_ERR_CUDA (-2)
+#define GSPEC_ERR_UNSUPPORTED (-3)
+#define GSPEC_ERR_STATE (-4)
+
+/* InputType of the reference template (edd/GatedSpectrometer.cuh:87-142). */
+#define GSPEC_SINGLE_POL 0 /* SinglePolarizationInput */
+#define GSPEC_DUAL_POL 1   /* DualPolarizationInput   */
+
+/* OutputType (edd/GatedSpectrometer.cuh:207-260). */
+#define GSPEC_POWER 0       /* GatedPowerSpectrumOutput */
+#define GSPEC_FULL_STOKES 1 /* GatedFullStokesOutput    */
+
+/* Gate-index convention. */
+#define GSPEC_INTENDED 0  /* item of the heap holding the sample; per-pol baselines */
+#define GSPEC_REFERENCE 1 /* the reference's literal indexing where it stays in bounds */
+
+/* Flags. */
+#define GSPEC_FLAG_SATURATION_RECORD 1u /* append n_out x {sat G0, sat G1} u64 to each output */
+
+typedef struct gspec_config {
+  /* DadaBufferLayout (edd/DadaBufferLayout.hpp:20-54): the reference reads the
+   * buffer size from the ring buffer (edd/src/DadaBufferLayout.cpp:17-39);
+   * here the caller passes it. */
+  uint64_t buffer_size;           /* bytes of one DADA data block */
+  uint64_t heap_size;             /* bytes of sample data per heap */
+  uint64_t n_side_channels;       /* uint64 items per heap */
+  /* GatedSpectrometer constructor arguments (edd/GatedSpectrometer.cuh:292-297). */
+  uint64_t selected_side_channel;
+  uint64_t selected_bit;
+  uint64_t fft_length;
+  uint64_t naccumulate;
+  uint32_t nbits;                 /* 8, 10 or 12 */
+  uint32_t input_type;            /* GSPEC_SINGLE_POL / GSPEC_DUAL_POL */
+  uint32_t output_type;           /* GSPEC_POWER / GSPEC_FULL_STOKES */
+  uint32_t convention;            /* GSPEC_INTENDED / GSPEC_REFERENCE */
+  float input_level;              /* logged only, as in the reference */
+  float output_level;
+  int32_t device;                 /* CUDA device ordinal */
+  uint32_t flags;
+} gspec_config;
+
+typedef struct gspec_info {
+  uint64_t nchans;                /* fft_length/2 + 1 */
+  uint64_t n_out;                 /* output spectra per output block */
+  uint64_t n_blocks;              /* input blocks integrated per output block */
+  uint64_t nsamps_per_pol;        /* samples per pol per input block */
+  uint64_t batch;                 /* FFT frames per pol per input block */
+  uint64_t output_bytes;          /* bytes handed to the handler per output block */
+  uint64_t record_bytes;          /* bytes per output spectrum record */
+  uint64_t device_bytes;          /* device memory held by the handle */
+  uint64_t fft_path;              /* 0 shared-memory FFT, 1 four-step FFT */
+  uint64_t n1, n2;                /* four-step split (0 for the shared-memory path) */
+} gspec_info;
+
+/* Output of one gspec_process call: when ready != 0 the handler must be
+ * called with (data, size) before the next gspec_process call. */
+typedef struct gspec_output {
+  char* data;
+  size_t size;
+  int ready;
+} gspec_output;
+
+typedef struct gspec_handle gspec_handle;
+
+/* Replaces the GatedSpectrometer constructor
+ * (edd/detail/GatedSpectrometer.cu:66-161).  Returns NULL on error and
+ * writes the reason into err (if err_len > 0). */
+gspec_handle* gspec_create(const gspec_config* cfg, char* err, size_t err_len);
+
+/* Replaces GatedSpectrometer::~GatedSpectrometer (edd/detail/GatedSpectrometer.cu:164-176). */
+void gspec_destroy(gspec_handle* h);
+
+/* Replaces GatedSpectrometer::init(RawBytes&) (edd/detail/GatedSpectrometer.cu:179-215):
+ * appends the spectrometer parameters to the NUL-terminated DADA header in
+ * place when they fit into total_bytes.  Returns GSPEC_OK, or GSPEC_STOP
+ * when the text did not fit (the reference logs a warning). */
+int gspec_init(gspec_handle* h, char* header, size_t total_bytes);
+
+/* Replaces GatedSpectrometer::operator()(RawBytes&)
+ * (edd/detail/GatedSpectrometer.cu:299-365) for a block in host memory
+ * (pinned or pageable).  The block is fully consumed when the call returns.
+ * Returns GSPEC_STOP when used_bytes differs from the buffer size. */
+int gspec_process(gspec_handle* h, const char* block, size_t used_bytes, gspec_output* out);
+
+/* Same for a block that already resides in device memory (RawBytes with
+ * on_device() == true). */
+int gspec_process_device(gspec_handle* h, const void* d_block, size_t used_bytes, gspec_output* out);
+
+/* One pass of the chain over one block in device memory, accumulated into a
+ * caller-owned device output buffer (gspec_info.output_bytes without the
+ * saturation record, host layout), on the caller's CUDA stream; updates the
+ * baselines.  No handler pipeline, no host copies.  The caller zeroes d_out
+ * at the start of an output block. */
+int gspec_run_block_device(gspec_handle* h, const void* d_block, void* d_out, void* cuda_stream);
+
+int gspec_get_info(const gspec_handle* h, gspec_info* info);
+const char* gspec_last_error(const gspec_handle* h);
+
+/* Baselines [npol][G0, G1] currently used for the next block (device copy
+ * synchronised to the host) and their override (tests). */
+int gspec_get_baselines(gspec_handle* h, float* out4);
+int gspec_set_baselines(gspec_handle* h, const float* in4);
+
+/* Saturation counts [n_out][G0, G1] of the last output handed out by
+ * gspec_process (new in this library; no counterpart in the reference). */
+int gspec_get_saturation(gspec_handle* h, uint64_t* out);
+
+/* Test entry points of single stages on device memory. */
+/* Unpacker::unpack<nbits> (edd/src/Unpacker.cu:124-140): contiguous packed
+ * big-endian samples -> float. */
+int gspec_unpack_device(const void* d_raw, uint32_t nbits, uint64_t nsamples, float* d_out, void* cuda_stream);
+/* gating (edd/src/GatedSpectrometer.cu:22-90) of a whole block with the
+ * handle's current baselines; d_gated is [npol][G0, G1][nsamps_per_pol]
+ * float.  Does not change the handle's state. */
+int gspec_gate_device(gspec_handle* h, const void* d_block, float* d_gated, void* cuda_stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GSPEC_H */

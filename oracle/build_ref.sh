@@ -1,0 +1,30 @@
+#!/usr/bin/env bash
+# Builds oracle/_ref/libref_host.so from the reference's own sources where
+# they lie (psrdada_cpp tree, default /root/reference), with the stub headers
+# in oracle/ref_shim/ standing in for googletest, Boost.Log and psrdada.
+# The library exports the reference's host-side C reference functions
+# (see oracle/ref_shim/ref_exports.cu); it is used only to pin the oracle.
+set -euo pipefail
+HERE="$(cd "$(dirname "$0")" && pwd)"
+REF="${1:-/root/reference}"
+OUT="$HERE/_ref"
+NVCC="${NVCC:-/usr/local/cuda/bin/nvcc}"
+[ -d "$REF/psrdada_cpp" ] || { echo "reference tree not found at $REF" >&2; exit 2; }
+mkdir -p "$OUT"
+EDD="$REF/psrdada_cpp/effelsberg/edd"
+FLAGS=(-std=c++17 -O2 -Xcompiler -fPIC -DENABLE_CUDA=1 -gencode arch=compute_103a,code=sm_103a
+       -I "$HERE/ref_shim" -I "$REF" -w)
+SRCS=("$EDD/test/src/UnpackerTester.cu" "$EDD/test/src/DetectorAccumulatorTester.cu"
+      "$EDD/src/Unpacker.cu" "$EDD/src/GatedSpectrometer.cu" "$REF/psrdada_cpp/src/raw_bytes.cpp"
+      "$HERE/ref_shim/ref_exports.cu" "$HERE/ref_shim/unused_symbols.cu")
+OBJS=()
+pids=()
+for s in "${SRCS[@]}"; do
+  b="$(basename "$s")"; o="$OUT/${b%.*}.o"
+  OBJS+=("$o")
+  "$NVCC" "${FLAGS[@]}" -x cu -c "$s" -o "$o" &
+  pids+=($!)
+done
+for p in "${pids[@]}"; do wait "$p"; done
+"$NVCC" -gencode arch=compute_103a,code=sm_103a -shared -o "$OUT/libref_host.so" "${OBJS[@]}" -lcudart
+echo "built $OUT/libref_host.so"

@@ -1,0 +1,10 @@
+"""GB300-native EDD gated spectrometer (drop-in for psrdada_cpp's GatedSpectrometer).
+
+The compute path is the CUDA library ``libgspec.so`` (C ABI in include/gspec.h);
+``gated_spectrometer`` mirrors the reference handler interface over it.
+"""
+from .gated_spectrometer import (  # noqa: F401
+    DadaBufferLayout, RawBytes, GatedSpectrometer, NullSink, CollectingSink, SimpleFileWriter,
+    GspecError, load_library, unpack_device, file_input_stream,
+    SINGLE_POL, DUAL_POL, POWER, FULL_STOKES, INTENDED, REFERENCE, FLAG_SATURATION_RECORD,
+)

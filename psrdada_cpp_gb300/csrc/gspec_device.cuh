@@ -1,0 +1,341 @@
+// Device building blocks of the gated spectrometer (sm_103a).
+//
+//  * bit-stream unpack of big-endian two's-complement 8/10/12-bit samples
+//    (the arithmetic of edd/src/Unpacker.cu:24-108 and
+//    edd/test/src/UnpackerTester.cu:41-201, written as funnel shifts over
+//    byte-swapped 32-bit words);
+//  * the side-channel gate (edd/src/GatedSpectrometer.cu:22-59) with the
+//    reference's exact float formula (v - b) * m + b;
+//  * register DFTs of radix 2/4/8/16 and a shared-memory Stockham FFT used
+//    by every FFT kernel of the library (replaces cuFFT R2C,
+//    edd/detail/GatedSpectrometer.cu:144-145,281-288).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gspec {
+
+// ---------------------------------------------------------------- complex
+struct __align__(8) cf { float x, y; };
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+// multiply by -i
+__device__ __forceinline__ float2 cmul_mi(float2 a) { return make_float2(a.y, -a.x); }
+
+// ------------------------------------------------------------ smem padding
+// One float2 of padding per 16 keeps the Stockham stores (stride R) and the
+// unpack stores (stride G) free of bank conflicts for R, G in {8, 16}.
+__device__ __forceinline__ int spad(int i) { return i + (i >> 4); }
+__host__ __device__ constexpr int spad_size(int n) { return n + (n >> 4); }
+
+// ------------------------------------------------------------- register DFTs
+// Forward DFT (W = exp(-2 pi i / R)), natural order in and out.
+__device__ __forceinline__ void dft2(float2& a, float2& b) {
+  float2 t = a;
+  a = cadd(t, b);
+  b = csub(t, b);
+}
+
+__device__ __forceinline__ void dft4(float2& v0, float2& v1, float2& v2, float2& v3) {
+  float2 t0 = cadd(v0, v2), t1 = csub(v0, v2);
+  float2 t2 = cadd(v1, v3), t3 = cmul_mi(csub(v1, v3));
+  v0 = cadd(t0, t2);
+  v2 = csub(t0, t2);
+  v1 = cadd(t1, t3);
+  v3 = csub(t1, t3);
+}
+
+constexpr float kS2 = 0.70710678118654752f;   // sqrt(1/2)
+constexpr float kC8 = 0.92387953251128674f;   // cos(pi/8)
+constexpr float kS8 = 0.38268343236508977f;   // sin(pi/8)
+
+// multiply by W8^1 = (1 - i)/sqrt2
+__device__ __forceinline__ float2 w8_1(float2 a) { return make_float2(kS2 * (a.x + a.y), kS2 * (a.y - a.x)); }
+// multiply by W8^3 = (-1 - i)/sqrt2
+__device__ __forceinline__ float2 w8_3(float2 a) { return make_float2(kS2 * (a.y - a.x), -kS2 * (a.x + a.y)); }
+// multiply by W16^1 = cos(pi/8) - i sin(pi/8)
+__device__ __forceinline__ float2 w16_1(float2 a) {
+  return make_float2(fmaf(a.x, kC8, a.y * kS8), fmaf(a.y, kC8, -a.x * kS8));
+}
+// multiply by W16^3 = sin(pi/8) - i cos(pi/8)
+__device__ __forceinline__ float2 w16_3(float2 a) {
+  return make_float2(fmaf(a.x, kS8, a.y * kC8), fmaf(a.y, kS8, -a.x * kC8));
+}
+// multiply by W16^9 = -W16^1
+__device__ __forceinline__ float2 w16_9(float2 a) {
+  return make_float2(-fmaf(a.x, kC8, a.y * kS8), -fmaf(a.y, kC8, -a.x * kS8));
+}
+
+__device__ __forceinline__ void dft8(float2 (&v)[8]) {
+  // 8 = 2 x 4: v[a + 2b], a in {0,1}, b in 0..3
+  dft4(v[0], v[2], v[4], v[6]);
+  dft4(v[1], v[3], v[5], v[7]);
+  // y[a][c] lives in v[a + 2c]; twiddle W8^(a*c)
+  v[3] = w8_1(v[3]);
+  v[5] = cmul_mi(v[5]);
+  v[7] = w8_3(v[7]);
+  // V[c + 4d] = y0[c] + W2^d y1[c]
+  float2 o[8];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    o[c] = cadd(v[2 * c], v[2 * c + 1]);
+    o[c + 4] = csub(v[2 * c], v[2 * c + 1]);
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = o[i];
+}
+
+__device__ __forceinline__ void dft16(float2 (&v)[16]) {
+  // 16 = 4 x 4: v[a + 4b]; stage 1 DFT4 over b for each a
+#pragma unroll
+  for (int a = 0; a < 4; ++a) dft4(v[a], v[a + 4], v[a + 8], v[a + 12]);
+  // y[a][c] in v[a + 4c]; twiddle W16^(a*c)
+  v[5] = w16_1(v[5]);                 // a1 c1
+  v[9] = w8_1(v[9]);                  // a1 c2 : W16^2
+  v[13] = w16_3(v[13]);               // a1 c3
+  v[6] = w8_1(v[6]);                  // a2 c1 : W16^2
+  v[10] = cmul_mi(v[10]);             // a2 c2 : W16^4
+  v[14] = w8_3(v[14]);                // a2 c3 : W16^6
+  v[7] = w16_3(v[7]);                 // a3 c1
+  v[11] = w8_3(v[11]);                // a3 c2 : W16^6
+  v[15] = w16_9(v[15]);               // a3 c3
+  // stage 2: DFT4 over a for each c; V[c + 4d]
+  float2 o[16];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    float2 y0 = v[4 * c], y1 = v[4 * c + 1], y2 = v[4 * c + 2], y3 = v[4 * c + 3];
+    dft4(y0, y1, y2, y3);
+    o[c] = y0;
+    o[c + 4] = y1;
+    o[c + 8] = y2;
+    o[c + 12] = y3;
+  }
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = o[i];
+}
+
+template <int R>
+__device__ __forceinline__ void dft(float2 (&v)[R]) {
+  if constexpr (R == 2) {
+    dft2(v[0], v[1]);
+  } else if constexpr (R == 4) {
+    dft4(v[0], v[1], v[2], v[3]);
+  } else if constexpr (R == 8) {
+    dft8(v);
+  } else {
+    static_assert(R == 16, "radix");
+    dft16(v);
+  }
+}
+
+// ------------------------------------------------------ Stockham FFT plan
+// N = 16^a * r, r in {1,2,4,8}: passes of radix 16 then one of radix r.
+__host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
+__host__ __device__ constexpr int pass_radix(int n, int ns) { return (n / ns) >= 16 ? 16 : (n / ns); }
+// offset (in float2) of the twiddle table of the pass whose span is ns
+__host__ __device__ constexpr int tw_offset(int n, int ns) {
+  int off = 0;
+  for (int s = 1; s < ns; s *= pass_radix(n, s)) {
+    if (s > 1) off += s * pass_radix(n, s);
+  }
+  return off;
+}
+__host__ __device__ constexpr int tw_size(int n) { return tw_offset(n, n); }
+
+// One in-place FFT of N points in padded shared memory S, done by the
+// T = N/P threads with index t of the calling group.  Every thread of the
+// block must call it the same number of times (it contains __syncthreads).
+// tw: per-pass tables, entry [k][q] = exp(-2 pi i q k / (ns R)) at
+// tw_offset(N, ns) + k*ns + q.
+template <int N, int P, int NS = 1>
+__device__ __forceinline__ void fft_smem(float2* S, const float2* __restrict__ tw, int t, bool active) {
+  if constexpr (NS < N) {
+    constexpr int R = pass_radix(N, NS);
+    constexpr int T = N / P;
+    constexpr int NB = P / R;
+    static_assert(P % R == 0, "points per thread must be a multiple of the radix");
+    float2 v[NB][R];
+    if (active) {
+#pragma unroll
+      for (int u = 0; u < NB; ++u) {
+        const int j = t + T * u;
+#pragma unroll
+        for (int k = 0; k < R; ++k) v[u][k] = S[spad(j + k * (N / R))];
+      }
+    }
+    __syncthreads();
+    if (active) {
+#pragma unroll
+      for (int u = 0; u < NB; ++u) {
+        const int j = t + T * u;
+        const int q = j & (NS - 1);
+        if constexpr (NS > 1) {
+          constexpr int TO = tw_offset(N, NS);
+#pragma unroll
+          for (int k = 1; k < R; ++k) v[u][k] = cmul(v[u][k], __ldg(&tw[TO + k * NS + q]));
+        }
+        dft<R>(v[u]);
+        const int base = (j - q) * R + q;
+#pragma unroll
+        for (int k = 0; k < R; ++k) S[spad(base + k * NS)] = v[u][k];
+      }
+    }
+    __syncthreads();
+    fft_smem<N, P, NS * R>(S, tw, t, active);
+  }
+}
+
+// ------------------------------------------------------------------ unpack
+// A group is the smallest whole number of samples that starts on a 64-bit
+// word: 8 samples / 8 bytes (8 bit), 32 / 40 (10 bit), 16 / 24 (12 bit).
+template <int NBITS> struct Group;
+template <> struct Group<8> { static constexpr int samples = 8, words = 1; };
+template <> struct Group<10> { static constexpr int samples = 32, words = 5; };
+template <> struct Group<12> { static constexpr int samples = 16, words = 3; };
+
+__device__ __forceinline__ uint32_t bswap32(uint32_t x) { return __byte_perm(x, 0, 0x0123); }
+
+// Unpack one group from `p` (8-byte aligned, global memory) into out[]
+// as signed integers.  The 64-bit words are read as little-endian 32-bit
+// halves and byte-swapped into a big-endian bit stream W[0..2*words).
+template <int NBITS>
+__device__ __forceinline__ void unpack_group(const uint8_t* __restrict__ p, int (&out)[Group<NBITS>::samples]) {
+  constexpr int NW = 2 * Group<NBITS>::words;
+  uint32_t W[NW + 1];
+  const uint2* q = reinterpret_cast<const uint2*>(p);
+#pragma unroll
+  for (int w = 0; w < Group<NBITS>::words; ++w) {
+    uint2 u = __ldg(q + w);
+    W[2 * w] = bswap32(u.x);
+    W[2 * w + 1] = bswap32(u.y);
+  }
+  W[NW] = 0;
+#pragma unroll
+  for (int i = 0; i < Group<NBITS>::samples; ++i) {
+    constexpr int dummy = 0;
+    (void)dummy;
+    const int bit = NBITS * i;
+    const int w = bit >> 5, sh = bit & 31;
+    // bits [sh, sh+32) of W[w]:W[w+1] (MSB first)
+    const uint32_t win = __funnelshift_l(W[w + 1], W[w], sh);
+    out[i] = static_cast<int32_t>(win) >> (32 - NBITS);
+  }
+}
+
+// ---------------------------------------------------------------- gating
+// Side-channel gate of one sample (edd/src/GatedSpectrometer.cu:49-52):
+//   G1 = (v - b1) * bit * !lost + b1 ;  G0 = (v - b0) * !bit * !lost + b0
+// evaluated with explicit round-to-nearest float ops so no contraction or
+// fast-math rewrite changes a bit of the result.
+__device__ __forceinline__ float gate_value(float v, float b, bool m) {
+  return m ? __fadd_rn(__fsub_rn(v, b), b) : b;
+}
+
+// Gate parameters shared by all kernels.
+struct GateParams {
+  const uint8_t* block;      // device copy of the whole DADA block
+  uint64_t sc_offset;        // byte offset of the side-channel items
+  uint32_t heap_size;        // bytes per heap
+  uint32_t nsc;              // items per heap
+  uint32_t sel;              // selected item
+  uint32_t bitpos;           // selected bit
+  uint32_t dual;             // 1: heaps and items alternate P0 P1
+  uint32_t convention;       // 0 intended, 1 reference
+  // intended: item = ((s * nbits) / (8 * heap_size)) * nsc + sel
+  // reference: item = (s / chunk) * step + ((s % chunk) / heap_size) * nsc + sel
+  uint32_t chunk;            // samples per gating chunk (reference)
+  uint32_t step;             // items per gating chunk (reference)
+  uint32_t nbits;
+};
+
+__device__ __forceinline__ uint32_t item_index(const GateParams& g, uint32_t s) {
+  if (g.convention == 1) {
+    const uint32_t j = s / g.chunk;
+    const uint32_t t = s - j * g.chunk;
+    return j * g.step + (t / g.heap_size) * g.nsc + g.sel;
+  }
+  const uint64_t bit = static_cast<uint64_t>(s) * g.nbits;
+  return static_cast<uint32_t>(bit / (8ull * g.heap_size)) * g.nsc + g.sel;
+}
+
+// Byte address of pol-stream byte b (dual-pol heaps alternate P0 P1).
+__device__ __forceinline__ const uint8_t* pol_byte(const GateParams& g, int pol, uint64_t b) {
+  if (!g.dual) return g.block + b;
+  const uint64_t h = b / g.heap_size;
+  return g.block + (2 * h + pol) * g.heap_size + (b - h * g.heap_size);
+}
+
+// Selected item of one pol after the dual-pol merge
+// (edd/src/GatedSpectrometer.cu:9-19 logical OR in the reference convention,
+// bitwise OR in the intended one).
+__device__ __forceinline__ uint64_t load_item(const GateParams& g, int pol, uint32_t idx) {
+  const uint64_t* items = reinterpret_cast<const uint64_t*>(g.block + g.sc_offset);
+  if (!g.dual) return __ldg(items + idx);
+  const uint64_t a = __ldg(items + 2ull * idx);
+  const uint64_t b = __ldg(items + 2ull * idx + 1);
+  if (g.convention == 1) return (a != 0 || b != 0) ? 1ull : 0ull;
+  (void)pol;
+  return a | b;
+}
+
+// Gate masks of an item: m0 = bit clear and heap kept, m1 = bit set and kept.
+__device__ __forceinline__ void item_masks(uint64_t item, uint32_t bitpos, bool& m0, bool& m1) {
+  const bool bit = (item >> bitpos) & 1ull;
+  const bool lost = (item >> 63) & 1ull;
+  m0 = !bit && !lost;
+  m1 = bit && !lost;
+}
+
+// Per-thread gate statistics.
+struct GateStats {
+  uint32_t n0 = 0, n1 = 0, sat0 = 0, sat1 = 0;
+  long long s0 = 0, s1 = 0;
+};
+
+// Unpack + gate one group of samples of one pol starting at pol sample s.
+// Writes gated G0/G1 floats into g0[], g1[] and updates the statistics.
+template <int NBITS>
+__device__ __forceinline__ void gate_group(const GateParams& g, int pol, uint32_t s, float b0, float b1,
+                                           float (&g0)[Group<NBITS>::samples], float (&g1)[Group<NBITS>::samples],
+                                           GateStats& st) {
+  constexpr int GS = Group<NBITS>::samples;
+  int v[GS];
+  const uint64_t byte0 = static_cast<uint64_t>(s) * NBITS / 8;
+  unpack_group<NBITS>(pol_byte(g, pol, byte0), v);
+  const uint32_t ia = item_index(g, s);
+  const uint32_t ib = item_index(g, s + GS - 1);
+  bool a0, a1;
+  item_masks(load_item(g, pol, ia), g.bitpos, a0, a1);
+  bool c0 = a0, c1 = a1;
+  uint32_t boundary = 0xffffffffu;
+  if (ib != ia) {
+    item_masks(load_item(g, pol, ib), g.bitpos, c0, c1);
+    // first sample whose item is ib
+    boundary = s;
+    while (boundary < s + GS && item_index(g, boundary) == ia) ++boundary;
+  }
+  constexpr int lo = -(1 << (NBITS - 1)), hi = (1 << (NBITS - 1)) - 1;
+#pragma unroll
+  for (int i = 0; i < GS; ++i) {
+    const bool second = (s + i) >= boundary;
+    const bool m0 = second ? c0 : a0;
+    const bool m1 = second ? c1 : a1;
+    const float vf = static_cast<float>(v[i]);
+    g0[i] = gate_value(vf, b0, m0);
+    g1[i] = gate_value(vf, b1, m1);
+    const bool sat = (v[i] == lo) | (v[i] == hi);
+    st.n0 += m0;
+    st.n1 += m1;
+    st.sat0 += (m0 && sat);
+    st.sat1 += (m1 && sat);
+    st.s0 += m0 ? v[i] : 0;
+    st.s1 += m1 ? v[i] : 0;
+  }
+}
+
+}  // namespace gspec

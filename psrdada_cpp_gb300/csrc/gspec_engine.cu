@@ -1,0 +1,547 @@
+// Host engine of the gated spectrometer and the C ABI of include/gspec.h.
+//
+// Mirrors GatedSpectrometer::operator() (edd/detail/GatedSpectrometer.cu:299-365):
+// block n is copied to the device at call n, processed at call n+1,
+// copied to the host at the next output swap and handed out one swap later,
+// so the sequence of handler calls and their contents is the reference's.
+// Differences: one H2D of the whole block per call (the dual-pol heap and
+// item de-interleave of edd/src/GatedSpectrometer.cu:261-306 happens in the
+// kernels' address arithmetic), one D2H per output block instead of 4*nOut
+// or 16*nOut small copies (:346-384, :430-527), the input block is consumed
+// before the call returns, and processing does not stall the host.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gspec.h"
+#include "gspec_kernels.cuh"
+
+using namespace gspec;
+
+struct gspec_handle {
+  gspec_config cfg{};
+  // layout (edd/src/DadaBufferLayout.cpp:17-39)
+  uint64_t n_heaps = 0, gap = 0, data_bytes = 0, sc_off = 0, sc_bytes = 0;
+  // derived (edd/detail/GatedSpectrometer.cu:99-153)
+  uint64_t nsamps = 0, items_per_pol = 0, n_blocks = 1, batch = 0, nacc = 0, n_out = 0, C = 0;
+  uint64_t rec = 0, out_bytes = 0, ext_bytes = 0;
+  int npol = 1;
+  bool dual = false;
+  int path = 0;
+  uint32_t N1 = 0, N2 = 0;
+  uint32_t slices = 1, frames_per_unit = 1;
+  uint32_t kchunk = 1;
+  int sm_count = 152;
+  std::string err;
+
+  uint8_t* d_in[2] = {nullptr, nullptr};
+  uint8_t* d_out[2] = {nullptr, nullptr};
+  unsigned long long* d_sat[2] = {nullptr, nullptr};
+  unsigned long long* d_sat_dev = nullptr;
+  char* h_out[2] = {nullptr, nullptr};
+  float* d_baselines = nullptr;
+  unsigned long long* d_pol_stats = nullptr;
+  float2* d_tw = nullptr;
+  float2* d_tw1 = nullptr;
+  float2* d_tw2 = nullptr;
+  float2* d_twA = nullptr;
+  float2* d_twB = nullptr;
+  float* d_partial = nullptr;
+  float2* d_scratch = nullptr;
+  cudaStream_t h2d = nullptr, proc = nullptr, d2h = nullptr;
+  cudaEvent_t ev_h2d[2] = {}, ev_in_free[2] = {}, ev_out_ready[2] = {};
+  int ia = 1, oa = 0, ha = 0, handed = -1;
+  bool host_written[2] = {false, false};
+  uint64_t call_count = 0;
+  uint64_t device_bytes = 0;
+};
+
+namespace {
+
+int set_err(gspec_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+bool cuda_ok(gspec_handle* h, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return true;
+  if (h) h->err = std::string(what) + ": " + cudaGetErrorString(e);
+  return false;
+}
+
+template <typename T>
+bool dalloc(gspec_handle* h, T** p, size_t bytes, const char* what) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), bytes);
+  if (e != cudaSuccess) {
+    h->err = std::string("cudaMalloc ") + what + ": " + cudaGetErrorString(e);
+    return false;
+  }
+  h->device_bytes += bytes;
+  return true;
+}
+
+int group_bytes(int nbits) { return nbits == 8 ? 8 : (nbits == 10 ? 40 : 24); }
+int group_samples(int nbits) { return nbits == 8 ? 8 : (nbits == 10 ? 32 : 16); }
+
+// Validates the configuration and fills the derived sizes.
+bool configure(gspec_handle* h) {
+  const gspec_config& c = h->cfg;
+  auto fail = [&](const std::string& m) {
+    h->err = m;
+    return false;
+  };
+  if (c.nbits != 8 && c.nbits != 10 && c.nbits != 12) return fail("nbits must be 8, 10 or 12");
+  if (c.input_type > 1 || c.output_type > 1) return fail("unknown input or output type");
+  if (c.input_type == GSPEC_DUAL_POL && c.output_type == GSPEC_POWER)
+    return fail("dual-pol power output is not implemented (as in the reference)");
+  if (c.input_type == GSPEC_SINGLE_POL && c.output_type == GSPEC_FULL_STOKES)
+    return fail("full-Stokes output needs dual-pol input");
+  if (c.convention > 1) return fail("unknown gate convention");
+  if (c.naccumulate == 0) return fail("naccumulate must be > 0");
+  if (c.selected_bit >= 64) return fail("selected_bit must be < 64");
+  if (c.n_side_channels == 0) return fail("at least one side-channel item per heap is required");
+  if (c.selected_side_channel >= c.n_side_channels) return fail("selected_side_channel out of range");
+  if (c.heap_size == 0) return fail("heap_size must be > 0");
+  const uint64_t N = c.fft_length;
+  if (N == 0 || (N & (N - 1))) return fail("fft_length must be a power of two");
+  if (small_fft_supported(static_cast<int>(N))) {
+    h->path = 0;
+  } else if (fourstep_supported(static_cast<int>(N))) {
+    h->path = 1;
+    h->N1 = fourstep_n1(static_cast<int>(N));
+    h->N2 = fourstep_n2(static_cast<int>(N));
+  } else {
+    return fail("fft_length must be in [32, 2^20]");
+  }
+  h->dual = c.input_type == GSPEC_DUAL_POL;
+  h->npol = h->dual ? 2 : 1;
+  const uint64_t scs = c.n_side_channels * 8;
+  h->n_heaps = c.buffer_size / (c.heap_size + scs);
+  if (h->n_heaps == 0) return fail("buffer holds no heap");
+  h->gap = c.buffer_size - h->n_heaps * (c.heap_size + scs);
+  h->data_bytes = h->n_heaps * c.heap_size;
+  h->sc_off = h->data_bytes + h->gap;
+  h->sc_bytes = scs * h->n_heaps;
+  if (h->dual && (h->n_heaps % 2)) return fail("dual-pol blocks need an even number of heaps");
+  const uint64_t pol_bytes = h->dual ? h->data_bytes / 2 : h->data_bytes;
+  if ((pol_bytes * 8) % c.nbits) return fail("pol data is not a whole number of samples");
+  h->nsamps = pol_bytes * 8 / c.nbits;
+  if (h->nsamps >= (1ull << 32)) return fail("more than 2^32 samples per pol");
+  h->items_per_pol = h->dual ? h->n_heaps * c.n_side_channels / 2 : h->n_heaps * c.n_side_channels;
+  const int gb = group_bytes(c.nbits);
+  if (h->dual && (c.heap_size % gb)) {
+    return fail("dual-pol heap size must be a multiple of " + std::to_string(gb) + " bytes");
+  }
+  if (c.heap_size < static_cast<uint64_t>(gb)) return fail("heap smaller than one unpack group");
+  // edd/detail/GatedSpectrometer.cu:114-130
+  const uint64_t per_out = N * c.naccumulate;
+  if (per_out <= h->nsamps) {
+    if (h->nsamps % per_out) return fail("samples per pol not a multiple of fft_length*naccumulate");
+    h->n_blocks = 1;
+  } else {
+    if (per_out % h->nsamps) return fail("fft_length*naccumulate not a multiple of samples per pol");
+    h->n_blocks = per_out / h->nsamps;
+    if (c.naccumulate % h->n_blocks || h->nsamps % N) return fail("block does not hold whole spectra");
+  }
+  h->batch = h->nsamps / N;
+  h->nacc = c.naccumulate / h->n_blocks;
+  h->n_out = h->batch / h->nacc;
+  h->C = N / 2 + 1;
+  h->rec = (h->dual ? 8 : 2) * (h->C * 4 + 8);
+  h->out_bytes = h->rec * h->n_out;
+  h->ext_bytes = h->n_out * 16;
+  if (c.convention == GSPEC_REFERENCE) {
+    const uint64_t L = h->nsamps / h->n_out;
+    const uint64_t step = h->items_per_pol / h->n_out;
+    if (step * 4096 != L) return fail("reference gating: chunk offset step*4096 does not tile the block");
+    const uint64_t last = (h->n_out - 1) * step + ((L - 1) / c.heap_size) * c.n_side_channels + c.selected_side_channel;
+    if (last >= h->items_per_pol) return fail("reference gating: side-channel index runs past the item array");
+  } else {
+    const uint64_t last = ((h->nsamps - 1) * c.nbits / (8 * c.heap_size)) * c.n_side_channels + c.selected_side_channel;
+    if (last >= h->items_per_pol) return fail("side-channel index runs past the item array");
+  }
+  return true;
+}
+
+GateParams gate_params(const gspec_handle* h, const uint8_t* block) {
+  GateParams g{};
+  g.block = block;
+  g.sc_offset = h->sc_off;
+  g.heap_size = static_cast<uint32_t>(h->cfg.heap_size);
+  g.nsc = static_cast<uint32_t>(h->cfg.n_side_channels);
+  g.sel = static_cast<uint32_t>(h->cfg.selected_side_channel);
+  g.bitpos = static_cast<uint32_t>(h->cfg.selected_bit);
+  g.dual = h->dual ? 1u : 0u;
+  g.convention = h->cfg.convention;
+  g.chunk = static_cast<uint32_t>(h->nsamps / h->n_out);
+  g.step = static_cast<uint32_t>(h->items_per_pol / h->n_out);
+  g.nbits = h->cfg.nbits;
+  return g;
+}
+
+cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out, unsigned long long* d_sat,
+                         cudaStream_t s) {
+  ChainParams p{};
+  p.g = gate_params(h, d_block);
+  p.baselines = h->d_baselines;
+  p.pol_stats = h->d_pol_stats;
+  p.sat = d_sat;
+  p.out = d_out;
+  p.partial = h->d_partial;
+  p.tw = h->d_tw;
+  p.out_rec = h->rec;
+  p.n_out = static_cast<uint32_t>(h->n_out);
+  p.nacc = static_cast<uint32_t>(h->nacc);
+  p.slices = h->slices;
+  p.frames_per_unit = h->frames_per_unit;
+  const int N = static_cast<int>(h->cfg.fft_length);
+  cudaError_t e;
+  if (h->path == 0) {
+    e = launch_small_chain(N, h->cfg.nbits, h->dual, p, s);
+    if (e != cudaSuccess) return e;
+    if (h->slices > 1) {
+      e = launch_reduce_partials(N, h->dual, p, s);
+      if (e != cudaSuccess) return e;
+    }
+  } else {
+    FourStepParams f{};
+    f.c = p;
+    f.scratch = h->d_scratch;
+    f.tw1 = h->d_tw1;
+    f.tw2 = h->d_tw2;
+    f.twA = h->d_twA;
+    f.twB = h->d_twB;
+    f.N1 = h->N1;
+    f.N2 = h->N2;
+    for (uint64_t k0 = 0; k0 < h->n_out; k0 += h->kchunk) {
+      const uint64_t nk = std::min<uint64_t>(h->kchunk, h->n_out - k0);
+      f.frame0 = static_cast<uint32_t>(k0 * h->nacc);
+      f.nframes = static_cast<uint32_t>(nk * h->nacc);
+      f.k0 = static_cast<uint32_t>(k0);
+      f.nk = static_cast<uint32_t>(nk);
+      e = launch_fourstep(N, h->cfg.nbits, h->dual, f, 0, s);
+      if (e != cudaSuccess) return e;
+      e = launch_fourstep(N, h->cfg.nbits, h->dual, f, 1, s);
+      if (e != cudaSuccess) return e;
+    }
+  }
+  return launch_finalize(p, h->npol, static_cast<int>(h->C), h->dual ? 1 : 0, static_cast<int>(h->cfg.convention),
+                         h->d_baselines, s);
+}
+
+uint64_t env_u64(const char* name, uint64_t dflt) {
+  const char* v = std::getenv(name);
+  if (!v || !*v) return dflt;
+  return std::strtoull(v, nullptr, 10);
+}
+
+void release(gspec_handle* h) {
+  if (!h) return;
+  for (int i = 0; i < 2; ++i) {
+    if (h->d_in[i]) cudaFree(h->d_in[i]);
+    if (h->d_out[i]) cudaFree(h->d_out[i]);
+    if (h->d_sat[i]) cudaFree(h->d_sat[i]);
+    if (h->h_out[i]) cudaFreeHost(h->h_out[i]);
+    if (h->ev_h2d[i]) cudaEventDestroy(h->ev_h2d[i]);
+    if (h->ev_in_free[i]) cudaEventDestroy(h->ev_in_free[i]);
+    if (h->ev_out_ready[i]) cudaEventDestroy(h->ev_out_ready[i]);
+  }
+  void* ptrs[] = {h->d_sat_dev, h->d_baselines, h->d_pol_stats, h->d_tw, h->d_tw1, h->d_tw2,
+                  h->d_twA,     h->d_twB,       h->d_partial,   h->d_scratch};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (h->h2d) cudaStreamDestroy(h->h2d);
+  if (h->proc) cudaStreamDestroy(h->proc);
+  if (h->d2h) cudaStreamDestroy(h->d2h);
+}
+
+int do_process(gspec_handle* h, const void* block, size_t used, gspec_output* out, bool on_device) {
+  if (!h || !out) return GSPEC_ERR_ARG;
+  out->ready = 0;
+  out->data = nullptr;
+  out->size = 0;
+  if (cudaSetDevice(h->cfg.device) != cudaSuccess) return set_err(h, GSPEC_ERR_CUDA, "cudaSetDevice failed");
+  ++h->call_count;
+  if (used != h->cfg.buffer_size) {
+    cudaStreamSynchronize(h->h2d);
+    cudaStreamSynchronize(h->proc);
+    cudaStreamSynchronize(h->d2h);
+    return set_err(h, GSPEC_STOP,
+                   "Unexpected Buffer Size - Got " + std::to_string(used) + " byte, expected " +
+                       std::to_string(h->cfg.buffer_size) + " byte");
+  }
+  if (!block) return set_err(h, GSPEC_ERR_ARG, "null block");
+  // input double buffer: buffer a receives block n (edd/detail/GatedSpectrometer.cu:314-316)
+  h->ia ^= 1;
+  const int ia = h->ia, ib = ia ^ 1;
+  if (!cuda_ok(h, cudaStreamWaitEvent(h->h2d, h->ev_in_free[ia], 0), "wait input") ||
+      !cuda_ok(h, cudaMemcpyAsync(h->d_in[ia], block, h->cfg.buffer_size,
+                                  on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->h2d),
+               "H2D block") ||
+      !cuda_ok(h, cudaEventRecord(h->ev_h2d[ia], h->h2d), "record h2d"))
+    return GSPEC_ERR_CUDA;
+  if (h->call_count == 1) {
+    return cuda_ok(h, cudaStreamSynchronize(h->h2d), "H2D") ? GSPEC_OK : GSPEC_ERR_CUDA;
+  }
+  const bool new_block = ((h->call_count - 1) % h->n_blocks) == 0;
+  if (new_block) {
+    if (!cuda_ok(h, cudaStreamSynchronize(h->d2h), "D2H")) return GSPEC_ERR_CUDA;
+    h->oa ^= 1;
+    h->ha ^= 1;
+    if (!cuda_ok(h, cudaMemsetAsync(h->d_out[h->oa], 0, h->out_bytes, h->proc), "zero output") ||
+        !cuda_ok(h, cudaMemsetAsync(h->d_sat[h->oa], 0, h->ext_bytes, h->proc), "zero saturation"))
+      return GSPEC_ERR_CUDA;
+  }
+  if (!cuda_ok(h, cudaStreamWaitEvent(h->proc, h->ev_h2d[ib], 0), "wait h2d") ||
+      !cuda_ok(h, launch_chain(h, h->d_in[ib], h->d_out[h->oa], h->d_sat[h->oa], h->proc), "chain kernels") ||
+      !cuda_ok(h, cudaEventRecord(h->ev_in_free[ib], h->proc), "record input free") ||
+      !cuda_ok(h, cudaEventRecord(h->ev_out_ready[h->oa], h->proc), "record output"))
+    return GSPEC_ERR_CUDA;
+  if (!(h->call_count == 2 || !new_block)) {
+    const int ob = h->oa ^ 1;
+    if (!cuda_ok(h, cudaStreamWaitEvent(h->d2h, h->ev_out_ready[ob], 0), "wait output") ||
+        !cuda_ok(h, cudaMemcpyAsync(h->h_out[h->ha], h->d_out[ob], h->out_bytes, cudaMemcpyDeviceToHost, h->d2h),
+                 "D2H output") ||
+        !cuda_ok(h, cudaMemcpyAsync(h->h_out[h->ha] + h->out_bytes, h->d_sat[ob], h->ext_bytes,
+                                    cudaMemcpyDeviceToHost, h->d2h),
+                 "D2H saturation"))
+      return GSPEC_ERR_CUDA;
+    h->host_written[h->ha] = true;
+    // the reference also hands out the never-written buffer at the first
+    // output swap when n_blocks >= 3; that call is skipped here
+    if (h->call_count != 3 && h->host_written[h->ha ^ 1]) {
+      h->handed = h->ha ^ 1;
+      out->data = h->h_out[h->handed];
+      out->size = h->out_bytes + ((h->cfg.flags & GSPEC_FLAG_SATURATION_RECORD) ? h->ext_bytes : 0);
+      out->ready = 1;
+    }
+  }
+  // the ring buffer releases the block after the call returns
+  if (!cuda_ok(h, cudaStreamSynchronize(h->h2d), "H2D")) return GSPEC_ERR_CUDA;
+  if (!cuda_ok(h, cudaPeekAtLastError(), "CUDA")) return GSPEC_ERR_CUDA;
+  return GSPEC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gspec_handle* gspec_create(const gspec_config* cfg, char* err, size_t err_len) {
+  auto report = [&](const std::string& m) {
+    if (err && err_len) {
+      std::snprintf(err, err_len, "%s", m.c_str());
+    }
+  };
+  if (!cfg) {
+    report("null config");
+    return nullptr;
+  }
+  gspec_handle* h = new gspec_handle();
+  h->cfg = *cfg;
+  if (!configure(h)) {
+    report(h->err);
+    delete h;
+    return nullptr;
+  }
+  auto bail = [&](const std::string& m) -> gspec_handle* {
+    report(m.empty() ? h->err : m);
+    release(h);
+    delete h;
+    return nullptr;
+  };
+  if (cudaSetDevice(cfg->device) != cudaSuccess) return bail("cudaSetDevice failed");
+  cudaDeviceProp prop{};
+  if (cudaGetDeviceProperties(&prop, cfg->device) == cudaSuccess) h->sm_count = prop.multiProcessorCount;
+  if (!cuda_ok(h, cudaStreamCreateWithFlags(&h->h2d, cudaStreamNonBlocking), "stream") ||
+      !cuda_ok(h, cudaStreamCreateWithFlags(&h->proc, cudaStreamNonBlocking), "stream") ||
+      !cuda_ok(h, cudaStreamCreateWithFlags(&h->d2h, cudaStreamNonBlocking), "stream"))
+    return bail("");
+  for (int i = 0; i < 2; ++i) {
+    if (!cuda_ok(h, cudaEventCreateWithFlags(&h->ev_h2d[i], cudaEventDisableTiming), "event") ||
+        !cuda_ok(h, cudaEventCreateWithFlags(&h->ev_in_free[i], cudaEventDisableTiming), "event") ||
+        !cuda_ok(h, cudaEventCreateWithFlags(&h->ev_out_ready[i], cudaEventDisableTiming), "event"))
+      return bail("");
+  }
+  const int N = static_cast<int>(cfg->fft_length);
+  const uint64_t vals = h->dual ? 8 : 2;
+  // work decomposition of the shared-memory path: slices per output spectrum
+  if (h->path == 0) {
+    const uint64_t target = env_u64("GSPEC_UNITS", 8ull * h->sm_count);
+    uint64_t s = env_u64("GSPEC_SLICES", 0);
+    if (s == 0) {
+      s = 1;
+      while (h->n_out * s < target && h->nacc % (2 * s) == 0) s *= 2;
+    }
+    if (h->nacc % s) return bail("GSPEC_SLICES must divide the frames per output spectrum");
+    h->slices = static_cast<uint32_t>(s);
+    h->frames_per_unit = static_cast<uint32_t>(h->nacc / s);
+  } else {
+    const uint64_t budget = env_u64("GSPEC_SCRATCH_MB", 512) << 20;
+    const uint64_t per_out = h->nacc * (h->dual ? 2 : 1) * static_cast<uint64_t>(N) * sizeof(float2);
+    uint64_t kc = budget / per_out;
+    if (kc < 1) kc = 1;
+    if (kc > h->n_out) kc = h->n_out;
+    h->kchunk = static_cast<uint32_t>(kc);
+  }
+  for (int i = 0; i < 2; ++i) {
+    if (!dalloc(h, &h->d_in[i], cfg->buffer_size, "input") || !dalloc(h, &h->d_out[i], h->out_bytes, "output") ||
+        !dalloc(h, &h->d_sat[i], h->ext_bytes, "saturation"))
+      return bail("");
+    if (!cuda_ok(h, cudaMallocHost(reinterpret_cast<void**>(&h->h_out[i]), h->out_bytes + h->ext_bytes),
+                 "pinned output"))
+      return bail("");
+    std::memset(h->h_out[i], 0, h->out_bytes + h->ext_bytes);
+    if (!cuda_ok(h, cudaMemset(h->d_out[i], 0, h->out_bytes), "memset") ||
+        !cuda_ok(h, cudaMemset(h->d_sat[i], 0, h->ext_bytes), "memset"))
+      return bail("");
+  }
+  if (!dalloc(h, &h->d_sat_dev, h->ext_bytes, "saturation") || !dalloc(h, &h->d_baselines, 4 * sizeof(float), "baselines") ||
+      !dalloc(h, &h->d_pol_stats, 2 * kPolStats * sizeof(unsigned long long), "stats"))
+    return bail("");
+  cudaMemset(h->d_baselines, 0, 4 * sizeof(float));
+  cudaMemset(h->d_pol_stats, 0, 2 * kPolStats * sizeof(unsigned long long));
+  cudaMemset(h->d_sat_dev, 0, h->ext_bytes);
+  if (h->path == 0) {
+    if (!dalloc(h, &h->d_tw, tw_size(N) * sizeof(float2), "twiddles")) return bail("");
+    if (!cuda_ok(h, launch_twiddles(N, h->d_tw, h->proc), "twiddles")) return bail("");
+    if (h->slices > 1 &&
+        !dalloc(h, &h->d_partial, h->n_out * h->slices * vals * h->C * sizeof(float), "partials"))
+      return bail("");
+  } else {
+    if (!dalloc(h, &h->d_tw1, tw_size(h->N1) * sizeof(float2), "twiddles") ||
+        !dalloc(h, &h->d_tw2, tw_size(h->N2) * sizeof(float2), "twiddles") ||
+        !dalloc(h, &h->d_twA, 1024 * sizeof(float2), "twiddles") ||
+        !dalloc(h, &h->d_twB, 1024 * sizeof(float2), "twiddles"))
+      return bail("");
+    if (!cuda_ok(h, launch_twiddles(h->N1, h->d_tw1, h->proc), "twiddles") ||
+        !cuda_ok(h, launch_twiddles(h->N2, h->d_tw2, h->proc), "twiddles") ||
+        !cuda_ok(h, launch_fourstep_twiddles(N, h->d_twA, h->d_twB, h->proc), "twiddles"))
+      return bail("");
+    const uint64_t frames = static_cast<uint64_t>(h->kchunk) * h->nacc;
+    if (!dalloc(h, &h->d_scratch, frames * (h->dual ? 2 : 1) * static_cast<uint64_t>(N) * sizeof(float2),
+                "four-step scratch"))
+      return bail("");
+  }
+  if (!cuda_ok(h, cudaStreamSynchronize(h->proc), "setup")) return bail("");
+  return h;
+}
+
+void gspec_destroy(gspec_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->cfg.device);
+  if (h->h2d) cudaStreamSynchronize(h->h2d);
+  if (h->proc) cudaStreamSynchronize(h->proc);
+  if (h->d2h) cudaStreamSynchronize(h->d2h);
+  release(h);
+  delete h;
+}
+
+int gspec_init(gspec_handle* h, char* header, size_t total_bytes) {
+  if (!h || !header) return GSPEC_ERR_ARG;
+  char text[512];
+  const int n = std::snprintf(text, sizeof(text),
+                              "\n# Gated spectrometer parameters: \n"
+                              "fft_length               %llu\n"
+                              "nchannels                %llu\n"
+                              "naccumulate              %llu\n"
+                              "selected_side_channel    %llu\n"
+                              "selected_bit             %llu\n"
+                              "output_bit_depth         %d\n"
+                              "full_stokes_output       %s\n",
+                              static_cast<unsigned long long>(h->cfg.fft_length),
+                              static_cast<unsigned long long>(h->C),
+                              static_cast<unsigned long long>(h->cfg.naccumulate),
+                              static_cast<unsigned long long>(h->cfg.selected_side_channel),
+                              static_cast<unsigned long long>(h->cfg.selected_bit), 32,
+                              h->cfg.output_type == GSPEC_FULL_STOKES ? "yes" : "no");
+  const size_t end = strnlen(header, total_bytes);
+  if (end + static_cast<size_t>(n) < total_bytes) {
+    std::memcpy(header + end, text, static_cast<size_t>(n) + 1);
+    return GSPEC_OK;
+  }
+  h->err = "Header of size " + std::to_string(total_bytes) + " bytes already contains " + std::to_string(end) +
+           " bytes. Cannot add gated spectrometer info of size " + std::to_string(n) + " bytes.";
+  return GSPEC_STOP;
+}
+
+int gspec_process(gspec_handle* h, const char* block, size_t used_bytes, gspec_output* out) {
+  return do_process(h, block, used_bytes, out, false);
+}
+
+int gspec_process_device(gspec_handle* h, const void* d_block, size_t used_bytes, gspec_output* out) {
+  return do_process(h, d_block, used_bytes, out, true);
+}
+
+int gspec_run_block_device(gspec_handle* h, const void* d_block, void* d_out, void* cuda_stream) {
+  if (!h || !d_block || !d_out) return GSPEC_ERR_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+  if (!cuda_ok(h, launch_chain(h, static_cast<const uint8_t*>(d_block), static_cast<uint8_t*>(d_out), h->d_sat_dev, s),
+               "chain kernels"))
+    return GSPEC_ERR_CUDA;
+  return GSPEC_OK;
+}
+
+int gspec_get_info(const gspec_handle* h, gspec_info* info) {
+  if (!h || !info) return GSPEC_ERR_ARG;
+  info->nchans = h->C;
+  info->n_out = h->n_out;
+  info->n_blocks = h->n_blocks;
+  info->nsamps_per_pol = h->nsamps;
+  info->batch = h->batch;
+  info->output_bytes = h->out_bytes + ((h->cfg.flags & GSPEC_FLAG_SATURATION_RECORD) ? h->ext_bytes : 0);
+  info->record_bytes = h->rec;
+  info->device_bytes = h->device_bytes;
+  info->fft_path = static_cast<uint64_t>(h->path);
+  info->n1 = h->N1;
+  info->n2 = h->N2;
+  return GSPEC_OK;
+}
+
+const char* gspec_last_error(const gspec_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int gspec_get_baselines(gspec_handle* h, float* out4) {
+  if (!h || !out4) return GSPEC_ERR_ARG;
+  if (!cuda_ok(h, cudaStreamSynchronize(h->proc), "sync") ||
+      !cuda_ok(h, cudaMemcpy(out4, h->d_baselines, 4 * sizeof(float), cudaMemcpyDeviceToHost), "baselines"))
+    return GSPEC_ERR_CUDA;
+  return GSPEC_OK;
+}
+
+int gspec_set_baselines(gspec_handle* h, const float* in4) {
+  if (!h || !in4) return GSPEC_ERR_ARG;
+  if (!cuda_ok(h, cudaStreamSynchronize(h->proc), "sync") ||
+      !cuda_ok(h, cudaMemcpy(h->d_baselines, in4, 4 * sizeof(float), cudaMemcpyHostToDevice), "baselines"))
+    return GSPEC_ERR_CUDA;
+  return GSPEC_OK;
+}
+
+int gspec_get_saturation(gspec_handle* h, uint64_t* out) {
+  if (!h || !out) return GSPEC_ERR_ARG;
+  if (h->handed < 0) return set_err(h, GSPEC_ERR_STATE, "no output handed out yet");
+  std::memcpy(out, h->h_out[h->handed] + h->out_bytes, h->ext_bytes);
+  return GSPEC_OK;
+}
+
+int gspec_unpack_device(const void* d_raw, uint32_t nbits, uint64_t nsamples, float* d_out, void* cuda_stream) {
+  if (!d_raw || !d_out) return GSPEC_ERR_ARG;
+  if (nbits != 8 && nbits != 10 && nbits != 12) return GSPEC_ERR_ARG;
+  if (nsamples % group_samples(static_cast<int>(nbits))) return GSPEC_ERR_ARG;
+  cudaError_t e = launch_unpack(static_cast<int>(nbits), static_cast<const uint8_t*>(d_raw), nsamples, d_out,
+                                static_cast<cudaStream_t>(cuda_stream));
+  return e == cudaSuccess ? GSPEC_OK : GSPEC_ERR_CUDA;
+}
+
+int gspec_gate_device(gspec_handle* h, const void* d_block, float* d_gated, void* cuda_stream) {
+  if (!h || !d_block || !d_gated) return GSPEC_ERR_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+  if (!cuda_ok(h, cudaStreamSynchronize(h->proc), "sync")) return GSPEC_ERR_CUDA;
+  if (!cuda_ok(h, launch_gate_debug(h->cfg.nbits, gate_params(h, static_cast<const uint8_t*>(d_block)),
+                                    h->d_baselines, h->npol, static_cast<uint32_t>(h->nsamps), d_gated, s),
+               "gate kernel"))
+    return GSPEC_ERR_CUDA;
+  return GSPEC_OK;
+}
+
+}  // extern "C"

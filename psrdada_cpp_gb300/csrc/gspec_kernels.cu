@@ -1,0 +1,469 @@
+// Gated-spectrometer kernels for sm_103a.
+//
+// Small FFT lengths (N <= 4096) run the whole chain of one frame inside one
+// CTA: unpack + gate (edd/src/Unpacker.cu:24-108, edd/src/GatedSpectrometer.cu:22-59)
+// into shared memory, one complex Stockham FFT per pair of real sequences
+// (replacing the two cuFFT R2C calls, edd/detail/GatedSpectrometer.cu:281-288),
+// and the detect (edd/DetectorAccumulator.cuh:40-61) or Stokes
+// (edd/src/GatedSpectrometer.cu:140-169) accumulation fused into the epilogue.
+//
+// Two real sequences a, b share one complex FFT of z = a + i b:
+//   A(k) = (Z(k) + conj Z(N-k)) / 2 ,  B(k) = (Z(k) - conj Z(N-k)) / (2i).
+// Single pol pairs the two gates of one frame; dual pol pairs the two pols of
+// one gate.
+#include "gspec_kernels.cuh"
+
+namespace gspec {
+
+// ------------------------------------------------------------------ helpers
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Reduce NV per-thread values over the block; thread v < NV of the block
+// receives total v in `out` (returns true for those threads).
+template <int NV>
+__device__ __forceinline__ bool block_sum_u64(unsigned long long (&vals)[NV], unsigned long long* red,
+                                             unsigned long long& out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    unsigned long long s = warp_sum_u64(vals[v]);
+    if (lane == 0) red[warp * NV + v] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    unsigned long long s = 0;
+    for (int w = 0; w < nwarps; ++w) s += red[w * NV + threadIdx.x];
+    out = s;
+  }
+  return threadIdx.x < NV;
+}
+
+// Add the block's gate statistics to the counters.
+//   per pol: n0, n1, s0, s1 -> pol_stats;  sum over pols: n0, n1 -> output
+//   record counters of spectrum k; sat0, sat1 -> sat[k].
+template <int NPOL>
+__device__ __forceinline__ void commit_stats(const ChainParams& p, const GateStats (&st)[NPOL], uint32_t k,
+                                             int vals_c, unsigned long long* red) {
+  constexpr int NV = 4 * NPOL + 4;
+  unsigned long long v[NV];
+#pragma unroll
+  for (int q = 0; q < NPOL; ++q) {
+    v[4 * q + 0] = st[q].n0;
+    v[4 * q + 1] = st[q].n1;
+    v[4 * q + 2] = static_cast<unsigned long long>(st[q].s0);
+    v[4 * q + 3] = static_cast<unsigned long long>(st[q].s1);
+  }
+  unsigned long long n0 = 0, n1 = 0, s0 = 0, s1 = 0;
+#pragma unroll
+  for (int q = 0; q < NPOL; ++q) {
+    n0 += st[q].n0;
+    n1 += st[q].n1;
+    s0 += st[q].sat0;
+    s1 += st[q].sat1;
+  }
+  v[4 * NPOL + 0] = n0;
+  v[4 * NPOL + 1] = n1;
+  v[4 * NPOL + 2] = s0;
+  v[4 * NPOL + 3] = s1;
+  unsigned long long tot;
+  if (block_sum_u64<NV>(v, red, tot)) {
+    const int i = threadIdx.x;
+    if (i < 4 * NPOL) {
+      if (tot) atomicAdd(p.pol_stats + i, tot);
+    } else {
+      const int j = i - 4 * NPOL;
+      if (j < 2) {
+        unsigned long long* cnt =
+            reinterpret_cast<unsigned long long*>(p.out + k * p.out_rec + static_cast<uint64_t>(vals_c) * 4);
+        if (tot) atomicAdd(cnt + j, tot);
+      } else {
+        if (tot) atomicAdd(p.sat + 2 * k + (j - 2), tot);
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------ small chain
+template <int N, bool DUAL>
+struct SmallCfg {
+  static constexpr int P = 16;
+  static constexpr int SEQ = DUAL ? 2 : 1;
+  static constexpr int T = N / P;
+  static constexpr int SLOT_THREADS = SEQ * T;
+  static constexpr int NSLOT = SLOT_THREADS >= 256 ? 1 : 256 / SLOT_THREADS;
+  static constexpr int THREADS = NSLOT * SLOT_THREADS;
+  static constexpr int C = N / 2 + 1;
+  static constexpr int VALS = DUAL ? 8 : 2;
+  static constexpr int SEQ_F2 = spad_size(N);
+  static constexpr size_t SEQ_BYTES = static_cast<size_t>(NSLOT) * SEQ * SEQ_F2 * sizeof(float2);
+  static constexpr size_t ACC_BYTES = static_cast<size_t>(NSLOT) * VALS * C * sizeof(float);
+  static constexpr size_t RED_BYTES = static_cast<size_t>(THREADS / 32) * 12 * sizeof(unsigned long long);
+  static constexpr size_t SMEM = SEQ_BYTES + ACC_BYTES + RED_BYTES;
+};
+
+// One CTA per work unit (output spectrum k, slice); the slice's frames are
+// processed NSLOT at a time, each slot accumulating its frames' spectra in
+// shared memory; slots are summed in a fixed order at the end, so results do
+// not depend on scheduling.
+template <int N, int NBITS, bool DUAL>
+__global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS)
+    small_chain_kernel(ChainParams p) {
+  using Cfg = SmallCfg<N, DUAL>;
+  constexpr int G = Group<NBITS>::samples;
+  constexpr int NG = N / G;
+  constexpr int C = Cfg::C;
+  constexpr int NPOL = DUAL ? 2 : 1;
+  static_assert(N % G == 0, "frame must hold whole unpack groups");
+
+  extern __shared__ float4 smem_f4[];
+  float2* S = reinterpret_cast<float2*>(smem_f4);
+  float* acc = reinterpret_cast<float*>(reinterpret_cast<char*>(smem_f4) + Cfg::SEQ_BYTES);
+  unsigned long long* red =
+      reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(smem_f4) + Cfg::SEQ_BYTES + Cfg::ACC_BYTES);
+
+  const int tid = threadIdx.x;
+  const int slot = tid / Cfg::SLOT_THREADS;
+  const int lt = tid - slot * Cfg::SLOT_THREADS;
+  const int seq = lt / Cfg::T;
+  const int t = lt - seq * Cfg::T;
+
+  const uint32_t unit = blockIdx.x;
+  const uint32_t k = unit / p.slices;
+  const uint32_t sl = unit - k * p.slices;
+  const uint32_t f0 = k * p.nacc + sl * p.frames_per_unit;
+
+  float bl[2 * NPOL];
+#pragma unroll
+  for (int i = 0; i < 2 * NPOL; ++i) bl[i] = p.baselines[i];
+
+  for (int i = tid; i < Cfg::NSLOT * Cfg::VALS * C; i += Cfg::THREADS) acc[i] = 0.f;
+
+  GateStats st[NPOL];
+  float2* S0 = S + (slot * Cfg::SEQ) * Cfg::SEQ_F2;
+  float2* S1 = S0 + Cfg::SEQ_F2;
+  float* A = acc + slot * Cfg::VALS * C;
+
+  for (uint32_t it = 0; it < p.frames_per_unit; it += Cfg::NSLOT) {
+    const uint32_t fl = it + slot;
+    const bool active = fl < p.frames_per_unit;
+    if (active) {
+      const uint32_t f = f0 + fl;
+      for (int gi = lt; gi < NG; gi += Cfg::SLOT_THREADS) {
+        const uint32_t s = f * N + gi * G;
+        float a0[G], a1[G];
+        gate_group<NBITS>(p.g, 0, s, bl[0], bl[1], a0, a1, st[0]);
+        if constexpr (DUAL) {
+          float c0[G], c1[G];
+          gate_group<NBITS>(p.g, 1, s, bl[2], bl[3], c0, c1, st[NPOL - 1]);
+#pragma unroll
+          for (int e = 0; e < G; ++e) {
+            S0[spad(gi * G + e)] = make_float2(a0[e], c0[e]);
+            S1[spad(gi * G + e)] = make_float2(a1[e], c1[e]);
+          }
+        } else {
+#pragma unroll
+          for (int e = 0; e < G; ++e) S0[spad(gi * G + e)] = make_float2(a0[e], a1[e]);
+        }
+      }
+    }
+    __syncthreads();
+    // FFT of every sequence of the slot (contains the barriers)
+    fft_smem<N, Cfg::P>(S0 + seq * Cfg::SEQ_F2, p.tw, t, active);
+    if (active) {
+      for (int c = lt; c < C; c += Cfg::SLOT_THREADS) {
+        const int cm = (N - c) & (N - 1);
+        if constexpr (!DUAL) {
+          const float2 a = S0[spad(c)], b = S0[spad(cm)];
+          // A = Z(c), B = conj Z(N-c)
+          const float sx = a.x + b.x, sy = a.y - b.y;
+          const float dx = a.x - b.x, dy = a.y + b.y;
+          A[c] += 0.25f * fmaf(sx, sx, sy * sy);
+          A[C + c] += 0.25f * fmaf(dx, dx, dy * dy);
+        } else {
+#pragma unroll
+          for (int gate = 0; gate < 2; ++gate) {
+            const float2* Z = gate ? S1 : S0;
+            const float2 a = Z[spad(c)], b = Z[spad(cm)];
+            const float p1x = 0.5f * (a.x + b.x), p1y = 0.5f * (a.y - b.y);
+            const float p2x = 0.5f * (a.y + b.y), p2y = -0.5f * (a.x - b.x);
+            const float a1 = fmaf(p1x, p1x, p1y * p1y);
+            const float a2 = fmaf(p2x, p2x, p2y * p2y);
+            A[(0 + gate) * C + c] += a1 + a2;
+            A[(2 + gate) * C + c] += a1 - a2;
+            A[(4 + gate) * C + c] += 2.f * fmaf(p1x, p2x, p1y * p2y);
+            A[(6 + gate) * C + c] += -2.f * fmaf(p1y, p2x, -p1x * p2y);
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+
+  // slots -> output (fixed order)
+  float* outf = reinterpret_cast<float*>(p.out + k * p.out_rec);
+  for (int i = tid; i < Cfg::VALS * C; i += Cfg::THREADS) {
+    float v = 0.f;
+#pragma unroll 4
+    for (int s = 0; s < Cfg::NSLOT; ++s) v += acc[s * Cfg::VALS * C + i];
+    if (p.slices == 1) {
+      outf[i] += v;
+    } else {
+      p.partial[(static_cast<size_t>(k) * p.slices + sl) * Cfg::VALS * C + i] = v;
+    }
+  }
+  commit_stats<NPOL>(p, st, k, Cfg::VALS * C, red);
+}
+
+// out[k][i] += sum_s partial[k][s][i]  (fixed order)
+__global__ void reduce_partials_kernel(ChainParams p, int vals_c) {
+  const uint32_t k = blockIdx.y;
+  float* outf = reinterpret_cast<float*>(p.out + k * p.out_rec);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < vals_c; i += gridDim.x * blockDim.x) {
+    float v = 0.f;
+    const float* src = p.partial + static_cast<size_t>(k) * p.slices * vals_c + i;
+    for (uint32_t s = 0; s < p.slices; ++s) v += src[static_cast<size_t>(s) * vals_c];
+    outf[i] += v;
+  }
+}
+
+// Baselines for the next block (edd/src/GatedSpectrometer.cu:98-118), with
+// exact integer sums, an FP64 division and a zero-count guard; then the
+// Stokes record's counter copies (edd/src/GatedSpectrometer.cu:485-525).
+__global__ void finalize_kernel(ChainParams p, int npol, int C, int dual, int convention, float* baselines_out) {
+  const int lane = threadIdx.x;
+  const int vals = dual ? 8 : 2;
+  unsigned long long t0 = 0, t1 = 0;
+  for (uint32_t k = lane; k < p.n_out; k += 32) {
+    const unsigned long long* cnt =
+        reinterpret_cast<const unsigned long long*>(p.out + k * p.out_rec + static_cast<uint64_t>(vals) * C * 4);
+    t0 += cnt[0];
+    t1 += cnt[1];
+  }
+  t0 = warp_sum_u64(t0);
+  t1 = warp_sum_u64(t1);
+  if (lane == 0) {
+    for (int pol = 0; pol < npol; ++pol) {
+      unsigned long long* ps = p.pol_stats + pol * kPolStats;
+      unsigned long long den0 = ps[0], den1 = ps[1];
+      if (convention == 1) {
+        // cumulative output counters at the time this pol's update ran
+        den0 = t0;
+        den1 = t1;
+        if (npol == 2 && pol == 0) {
+          den0 -= p.pol_stats[kPolStats + 0];
+          den1 -= p.pol_stats[kPolStats + 1];
+        }
+      }
+      const long long s0 = static_cast<long long>(ps[2]);
+      const long long s1 = static_cast<long long>(ps[3]);
+      baselines_out[2 * pol + 0] = den0 ? static_cast<float>(static_cast<double>(s0) / static_cast<double>(den0)) : 0.f;
+      baselines_out[2 * pol + 1] = den1 ? static_cast<float>(static_cast<double>(s1) / static_cast<double>(den1)) : 0.f;
+    }
+  }
+  __syncwarp();
+  if (lane == 0) {
+    for (int i = 0; i < npol * kPolStats; ++i) p.pol_stats[i] = 0;
+  }
+  if (dual) {
+    for (uint32_t k = lane; k < p.n_out; k += 32) {
+      unsigned long long* cnt =
+          reinterpret_cast<unsigned long long*>(p.out + k * p.out_rec + static_cast<uint64_t>(vals) * C * 4);
+      for (int r = 1; r < 4; ++r) {
+        cnt[2 * r] = cnt[0];
+        cnt[2 * r + 1] = cnt[1];
+      }
+    }
+  }
+}
+
+// --------------------------------------------------------------- twiddles
+// FP64 twiddles (sincospi) rounded once to FP32.
+__global__ void twiddle_pass_kernel(float2* tw, int ns, int r) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ns * r) return;
+  const int kk = i / ns, q = i - kk * ns;
+  double s, c;
+  sincospi(-2.0 * static_cast<double>(q) * kk / (static_cast<double>(ns) * r), &s, &c);
+  tw[i] = make_float2(static_cast<float>(c), static_cast<float>(s));
+}
+
+__global__ void twiddle_split_kernel(float2* twA, float2* twB, int N) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nhi = (N + 1023) / 1024;
+  double s, c;
+  if (i < 1024) {
+    sincospi(-2.0 * static_cast<double>(i) / N, &s, &c);
+    twB[i] = make_float2(static_cast<float>(c), static_cast<float>(s));
+  }
+  if (i < nhi) {
+    sincospi(-2.0 * static_cast<double>(i) * 1024.0 / N, &s, &c);
+    twA[i] = make_float2(static_cast<float>(c), static_cast<float>(s));
+  }
+}
+
+// ------------------------------------------------------------ debug / unpack
+template <int NBITS>
+__global__ void gate_debug_kernel(GateParams g, const float* baselines, int npol, uint32_t nsamps, float* out) {
+  constexpr int G = Group<NBITS>::samples;
+  const uint32_t ngroups = nsamps / G;
+  for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < ngroups; gi += gridDim.x * blockDim.x) {
+    const uint32_t s = gi * G;
+    for (int pol = 0; pol < npol; ++pol) {
+      float a0[G], a1[G];
+      GateStats st;
+      gate_group<NBITS>(g, pol, s, baselines[2 * pol], baselines[2 * pol + 1], a0, a1, st);
+      float* o0 = out + static_cast<size_t>(2 * pol) * nsamps + s;
+      float* o1 = out + static_cast<size_t>(2 * pol + 1) * nsamps + s;
+#pragma unroll
+      for (int e = 0; e < G; ++e) {
+        o0[e] = a0[e];
+        o1[e] = a1[e];
+      }
+    }
+  }
+}
+
+template <int NBITS>
+__global__ void unpack_kernel(const uint8_t* raw, uint64_t ngroups, float* out) {
+  constexpr int G = Group<NBITS>::samples;
+  constexpr int GB = Group<NBITS>::words * 8;
+  for (uint64_t gi = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; gi < ngroups;
+       gi += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    int v[G];
+    unpack_group<NBITS>(raw + gi * GB, v);
+#pragma unroll
+    for (int e = 0; e < G; ++e) out[gi * G + e] = static_cast<float>(v[e]);
+  }
+}
+
+// ------------------------------------------------------------ dispatch
+template <int N, bool DUAL>
+static cudaError_t launch_small_t(int nbits, const ChainParams& p, cudaStream_t s) {
+  using Cfg = SmallCfg<N, DUAL>;
+  const unsigned grid = p.n_out * p.slices;
+  auto run = [&](auto kern) -> cudaError_t {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(Cfg::SMEM));
+    if (e != cudaSuccess) return e;
+    kern<<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(p);
+    return cudaGetLastError();
+  };
+  switch (nbits) {
+    case 8: return run(small_chain_kernel<N, 8, DUAL>);
+    case 10: return run(small_chain_kernel<N, 10, DUAL>);
+    case 12: return run(small_chain_kernel<N, 12, DUAL>);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <bool DUAL>
+static cudaError_t launch_small_d(int N, int nbits, const ChainParams& p, cudaStream_t s) {
+  switch (N) {
+    case 32: return launch_small_t<32, DUAL>(nbits, p, s);
+    case 64: return launch_small_t<64, DUAL>(nbits, p, s);
+    case 128: return launch_small_t<128, DUAL>(nbits, p, s);
+    case 256: return launch_small_t<256, DUAL>(nbits, p, s);
+    case 512: return launch_small_t<512, DUAL>(nbits, p, s);
+    case 1024: return launch_small_t<1024, DUAL>(nbits, p, s);
+    case 2048: return launch_small_t<2048, DUAL>(nbits, p, s);
+    case 4096: return launch_small_t<4096, DUAL>(nbits, p, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+bool small_fft_supported(int N) { return N >= 32 && N <= 4096 && (N & (N - 1)) == 0; }
+
+template <bool DUAL>
+static void small_cfg_query(int N, int& threads, size_t& smem) {
+#define GSPEC_Q(NN)                          \
+  case NN:                                   \
+    threads = SmallCfg<NN, DUAL>::THREADS;   \
+    smem = SmallCfg<NN, DUAL>::SMEM;         \
+    return;
+  switch (N) {
+    GSPEC_Q(32) GSPEC_Q(64) GSPEC_Q(128) GSPEC_Q(256) GSPEC_Q(512) GSPEC_Q(1024) GSPEC_Q(2048) GSPEC_Q(4096)
+  }
+#undef GSPEC_Q
+  threads = 0;
+  smem = 0;
+}
+
+int small_fft_threads(int N, bool dual) {
+  int t;
+  size_t s;
+  if (dual) small_cfg_query<true>(N, t, s); else small_cfg_query<false>(N, t, s);
+  return t;
+}
+
+size_t small_fft_smem(int N, bool dual) {
+  int t;
+  size_t s;
+  if (dual) small_cfg_query<true>(N, t, s); else small_cfg_query<false>(N, t, s);
+  return s;
+}
+
+cudaError_t launch_small_chain(int N, int nbits, bool dual, const ChainParams& p, cudaStream_t s) {
+  return dual ? launch_small_d<true>(N, nbits, p, s) : launch_small_d<false>(N, nbits, p, s);
+}
+
+cudaError_t launch_reduce_partials(int N, bool dual, const ChainParams& p, cudaStream_t s) {
+  const int vals_c = (dual ? 8 : 2) * (N / 2 + 1);
+  dim3 grid((vals_c + 255) / 256, p.n_out);
+  reduce_partials_kernel<<<grid, 256, 0, s>>>(p, vals_c);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const ChainParams& p, int npol, int C, int dual, int convention, float* baselines_out,
+                            cudaStream_t s) {
+  finalize_kernel<<<1, 32, 0, s>>>(p, npol, C, dual, convention, baselines_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_twiddles(int N, float2* tw, cudaStream_t s) {
+  for (int ns = 1; ns < N; ns *= pass_radix(N, ns)) {
+    const int r = pass_radix(N, ns);
+    if (ns == 1) continue;
+    const int off = tw_offset(N, ns);
+    const int n = ns * r;
+    twiddle_pass_kernel<<<(n + 255) / 256, 256, 0, s>>>(tw + off, ns, r);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_fourstep_twiddles(int N, float2* twA, float2* twB, cudaStream_t s) {
+  twiddle_split_kernel<<<4, 256, 0, s>>>(twA, twB, N);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gate_debug(int nbits, const GateParams& g, const float* baselines, int npol, uint32_t nsamps,
+                              float* out, cudaStream_t s) {
+  const int grid = 4 * 152, block = 256;
+  switch (nbits) {
+    case 8: gate_debug_kernel<8><<<grid, block, 0, s>>>(g, baselines, npol, nsamps, out); break;
+    case 10: gate_debug_kernel<10><<<grid, block, 0, s>>>(g, baselines, npol, nsamps, out); break;
+    case 12: gate_debug_kernel<12><<<grid, block, 0, s>>>(g, baselines, npol, nsamps, out); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_unpack(int nbits, const uint8_t* raw, uint64_t nsamples, float* out, cudaStream_t s) {
+  const int grid = 4 * 152, block = 256;
+  switch (nbits) {
+    case 8: unpack_kernel<8><<<grid, block, 0, s>>>(raw, nsamples / Group<8>::samples, out); break;
+    case 10: unpack_kernel<10><<<grid, block, 0, s>>>(raw, nsamples / Group<10>::samples, out); break;
+    case 12: unpack_kernel<12><<<grid, block, 0, s>>>(raw, nsamples / Group<12>::samples, out); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace gspec

@@ -1,0 +1,63 @@
+// Kernel parameter blocks and launch helpers shared by the kernels and the
+// host engine.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "gspec_device.cuh"
+
+namespace gspec {
+
+// Per-pol statistics of the block being processed (reset by finalize):
+// [pol][0] n0, [1] n1, [2] sum0 (two's complement), [3] sum1.
+constexpr int kPolStats = 4;
+
+struct ChainParams {
+  GateParams g;
+  const float* baselines;          // [npol][2]: G0, G1 baselines used for this block
+  unsigned long long* pol_stats;   // [npol][kPolStats]
+  unsigned long long* sat;         // [n_out][2] saturation counts (G0, G1)
+  uint8_t* out;                    // output accumulation buffer, host layout
+  float* partial;                  // [n_out][slices][VALS][C] (slices > 1)
+  const float2* tw;                // Stockham tables of the FFT length (small path)
+  uint64_t out_rec;                // bytes per output record
+  uint32_t n_out;
+  uint32_t nacc;                   // frames per output spectrum per block
+  uint32_t slices;                 // work units per output spectrum
+  uint32_t frames_per_unit;
+};
+
+// Large-N (four-step) parameters.
+struct FourStepParams {
+  ChainParams c;
+  float2* scratch;                 // [frames][SEQ][N1][N2] complex after pass A
+  const float2* tw1;               // Stockham tables of N1
+  const float2* tw2;               // Stockham tables of N2
+  const float2* twA;               // W_N^(m_hi * 1024) , m_hi < N/1024
+  const float2* twB;               // W_N^(m_lo), m_lo < 1024
+  uint32_t N1, N2;                 // N = N1 * N2; input sample n = N2*n1 + n2
+  uint32_t frame0;                 // first frame held in scratch
+  uint32_t nframes;                // frames of this launch (pass A)
+  uint32_t k0, nk;                 // output spectra of this launch (pass B)
+};
+
+// Host-side launchers (gspec_kernels.cu).
+cudaError_t launch_small_chain(int N, int nbits, bool dual, const ChainParams& p, cudaStream_t s);
+cudaError_t launch_reduce_partials(int N, bool dual, const ChainParams& p, cudaStream_t s);
+cudaError_t launch_finalize(const ChainParams& p, int npol, int C, int dual, int convention, float* baselines_out,
+                            cudaStream_t s);
+cudaError_t launch_twiddles(int N, float2* tw, cudaStream_t s);
+cudaError_t launch_fourstep_twiddles(int N, float2* twA, float2* twB, cudaStream_t s);
+cudaError_t launch_gate_debug(int nbits, const GateParams& g, const float* baselines, int npol, uint32_t nsamps,
+                              float* out, cudaStream_t s);
+cudaError_t launch_unpack(int nbits, const uint8_t* raw, uint64_t nsamples, float* out, cudaStream_t s);
+cudaError_t launch_fourstep(int N, int nbits, bool dual, const FourStepParams& p, int pass, cudaStream_t s);
+
+int small_fft_threads(int N, bool dual);
+size_t small_fft_smem(int N, bool dual);
+bool small_fft_supported(int N);
+bool fourstep_supported(int N);
+int fourstep_n1(int N);
+int fourstep_n2(int N);
+
+}  // namespace gspec
