@@ -1,0 +1,467 @@
+"""Throughput benchmark of the GB300 gated spectrometer.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c2|c1|c3] [--impl gb300|reference]
+
+One step = one DADA block of the workload through the whole chain (unpack,
+gate, R2C, Stokes/power accumulate).  Default workload: dual-pol 12-bit gated
+Stokes, fft 2^16, naccumulate 32, 2^26 samples per pol per block.
+
+* ``value``   device throughput, input Gsamples/s (both pols), inputs resident
+              in HBM: K blocks through gspec_run_block_device on the stream
+              the kernels run on, timed with CUDA events.  Two distinct
+              201 MB blocks alternate, so every step reads inputs larger than
+              L2.
+* ``e2e``     the same metric through the public handler API
+              (GatedSpectrometer.__call__ -> gspec_process) with blocks in
+              pinned host memory: every step copies its block host->device and
+              the pipeline copies one output block device->host.
+* ``roofline`` per-kernel CUDA-event times of a profiled pass; the dominant
+              kernel's algorithmic bytes per launch over its mean duration.
+* ``cpu_baseline`` the C/OpenMP restatement of the chain (oracle/gspec_cpu.c)
+              on this host's cores, on a bounded sample of the workload.
+
+``--impl reference`` times that CPU restatement alone (the reference has no
+CPU implementation of its own and its GPU code cannot be built here; see
+the design doc) on the same metric, each step one output spectrum's worth of
+input.  Under torchrun every rank runs its own stream on its own GPU
+(replicas, weak scaling); rank 0 prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "input Gsamples/s gated Stokes, BF16-TC vs FP32 at ≤1e-4 err; p99 block latency"
+UNIT = "Gsamples/s"
+FALLBACK_HBM_GBS = 6800.0
+
+
+# ------------------------------------------------------------------ helpers
+def workload(name: str):
+    from psrdada_cpp_gb300 import synth
+    if name == "c1":
+        return synth.config1(), "c1"
+    if name == "c3":
+        return synth.config3(), "c3"
+    return synth.config2(), "c2"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(backend: str):
+    import torch.distributed as dist
+    ws, rank, _ = dist_env()
+    if ws > 1 and not dist.is_initialized():
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        os.environ.setdefault("MASTER_PORT", "29511")
+        dist.init_process_group(backend=backend, rank=rank, world_size=ws)
+    return ws, rank
+
+
+def dist_barrier():
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
+
+
+def dist_max(x: float, device=None) -> float:
+    """Maximum of x over ranks (x itself on a single process)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_sum(x: float, device=None) -> float:
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        try:
+            with open(path) as f:
+                d = json.load(f)
+            for key in ("hbm_gbs", "hbm_GBs", "hbm"):
+                if key in d:
+                    return float(d[key]), "measured", d
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback", {}
+
+
+def ncu_traffic(kernel: str, workload_name: str):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            if line.startswith("#"):
+                continue
+            kv = dict(p.split("=", 1) for p in line.split() if "=" in p)
+            if kv.get("kernel") == kernel and kv.get("workload") == workload_name:
+                try:
+                    return float(kv["dram_bytes_per_launch"])
+                except (KeyError, ValueError):
+                    return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while running."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append((time.time(), line.strip()))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+
+    def summary(self, t0: float, t1: float):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ts, line in self.lines:
+            if not (t0 <= ts <= t1 + 0.06):
+                continue
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def sample_spec(spec, n_out: int):
+    """A bounded sample of the workload: the same stream with fewer output
+    spectra per block."""
+    from psrdada_cpp_gb300 import synth
+    import dataclasses
+    per_out = spec.fft_length * spec.naccumulate
+    return dataclasses.replace(spec, name=spec.name + f"_sample{n_out}", samples_per_pol=per_out * n_out)
+
+
+def cpu_chain_rate(spec, kind: str, seconds: float = 12.0, max_blocks: int = 64):
+    """Times the C restatement on all host cores; returns (Gsamples/s, cores,
+    sample description)."""
+    from oracle import gspec_cpu
+    from psrdada_cpp_gb300 import synth
+    cores = cpu_cores()
+    n_out = max(1, min(4, spec.samples_per_pol // (spec.fft_length * spec.naccumulate)))
+    sub = sample_spec(spec, n_out) if spec.samples_per_pol > spec.fft_length * spec.naccumulate else spec
+    chain = gspec_cpu.CpuChain(sub, nthreads=cores)
+    blocks = [synth.make_block(sub, seed=1, block_index=i, kind=kind) for i in range(2)]
+    chain.run_block(blocks[0])                       # warm-up
+    n, t0 = 0, time.perf_counter()
+    while n < max_blocks:
+        chain.zero()
+        chain.run_block(blocks[n % 2])
+        n += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    samples = n * sub.samples_per_pol * sub.npol
+    desc = (f"{n} blocks of {sub.samples_per_pol} samples/pol ({n_out} output spectra each) of {spec.name}, "
+            f"{dt:.1f} s on {cores} threads (parallel over the frames of each output spectrum)")
+    return samples / dt / 1e9, cores, desc
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_gpu(args):
+    import torch
+    ws, rank = dist_init("nccl")
+    _, _, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    import psrdada_cpp_gb300 as G
+    from psrdada_cpp_gb300 import synth
+
+    spec, kind = workload(args.workload)
+    samples_per_step = spec.samples_per_pol * spec.npol
+    lay = G.DadaBufferLayout(spec.buffer_size, spec.heap_size, spec.n_side_channels)
+    mk = dict(input_type=G.DUAL_POL if spec.dual_pol else G.SINGLE_POL, device=local)
+    gs = G.GatedSpectrometer(lay, 0, 0, spec.fft_length, spec.naccumulate, spec.nbits, 100.0, 100.0,
+                             G.NullSink(), **mk)
+    info = gs.info()
+    host_blocks = [synth.make_block(spec, seed=1 + rank, block_index=i, kind=kind) for i in range(2)]
+    d_blocks = [torch.from_numpy(b).to(dev) for b in host_blocks]
+    d_out = torch.zeros(int(info.output_bytes), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+
+    def step(i):
+        if i % int(info.n_blocks) == 0:
+            d_out.zero_()
+        gs.run_block_device(d_blocks[i % 2].data_ptr(), d_out.data_ptr(), sptr)
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize(dev)
+
+    # ---- device throughput (value)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    launches0 = gs.info().kernel_launches
+    dist_barrier()
+    torch.cuda.synchronize(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    tw0 = time.time()
+    ev0.record(stream)
+    for i in range(args.steps):
+        step(i)
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
+    tw1 = time.time()
+    dist_barrier()
+    launches = gs.info().kernel_launches - launches0
+    clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    ms_max = dist_max(ms, dev)
+    total_samples = dist_sum(samples_per_step * args.steps, dev)
+    value = total_samples / (ms_max / 1e3) / 1e9
+    clk = clocks.summary(tw0, tw1)
+
+    # ---- per-kernel profile (roofline)
+    gs.reset_profile()
+    gs.set_profiling(True)
+    nprof = max(4, min(32, args.steps))
+    for i in range(nprof):
+        step(i)
+    prof = gs.profile()
+    gs.set_profiling(False)
+    kernels = {k: v for k, v in prof.items() if v[1] > 0}
+    tot_ms = sum(v[2] for v in kernels.values())
+    dom = max(kernels, key=lambda k: kernels[k][2])
+    d_launches, d_timed, d_ms = kernels[dom]
+    per_launch_ms = d_ms / d_timed
+    in_bytes = spec.buffer_size
+    out_bytes = int(info.output_bytes)
+    launches_per_block = {k: v[1] / nprof for k, v in kernels.items()}
+    if dom in ("fourstep_a", "small_chain"):
+        alg_bytes_launch = (in_bytes + (out_bytes if dom == "small_chain" else 0)) / launches_per_block[dom]
+    elif dom == "fourstep_b":
+        alg_bytes_launch = out_bytes / launches_per_block[dom]
+    else:
+        alg_bytes_launch = (in_bytes + out_bytes) / launches_per_block[dom]
+    peak, peak_kind, _ = measured_peaks()
+    achieved = alg_bytes_launch / (per_launch_ms / 1e3) / 1e9
+    chain_ms = tot_ms / nprof
+    chain_gbs = (in_bytes + out_bytes) / (chain_ms / 1e3) / 1e9
+    N = spec.fft_length
+    seqs = spec.npol                                     # complex FFTs per frame (pair trick)
+    fft_flops = 5.0 * N * math.log2(N) * (spec.samples_per_pol // N) * seqs
+    roofline = {
+        "bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+        "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} copy bandwidth",
+        "traffic": ncu_traffic(dom, spec.name),
+        "algorithmic_bytes_per_launch": int(alg_bytes_launch), "mean_launch_ms": round(per_launch_ms, 4),
+        "chain": {"ms_per_block": round(chain_ms, 4), "algorithmic_bytes_per_block": in_bytes + out_bytes,
+                  "achieved_GBs": round(chain_gbs, 1), "frac": round(chain_gbs / peak, 4)},
+        "kernels": {k: {"launches_per_block": round(launches_per_block[k], 3),
+                        "mean_ms": round(v[2] / v[1], 4), "share": round(v[2] / tot_ms, 4)}
+                    for k, v in kernels.items()},
+        "fp32_fft": {"nominal_flops_per_block": fft_flops,
+                     "achieved_tflops": round(fft_flops / (chain_ms / 1e3) / 1e12, 2)},
+    }
+
+    # ---- end to end through the handler API, pinned host blocks
+    e2e = None
+    lat = []
+    if not args.no_e2e:
+        pinned = []
+        for b in host_blocks:
+            t = torch.empty(b.size, dtype=torch.uint8, pin_memory=True)
+            t.numpy()[:] = b
+            pinned.append(t)
+        sink = G.NullSink()
+        ge = G.GatedSpectrometer(lay, 0, 0, spec.fft_length, spec.naccumulate, spec.nbits, 100.0, 100.0, sink, **mk)
+        raws = [G.RawBytes(p.numpy()) for p in pinned]
+        for i in range(max(3, args.warmup)):
+            ge(raws[i % 2])
+        torch.cuda.synchronize(dev)
+        ke = max(8, min(args.steps, 400))
+        dist_barrier()
+        t0 = time.perf_counter()
+        for i in range(ke):
+            c0 = time.perf_counter()
+            ge(raws[i % 2])
+            lat.append((time.perf_counter() - c0) * 1e3)
+        torch.cuda.synchronize(dev)
+        t1 = time.perf_counter()
+        dist_barrier()
+        e_s = dist_max(t1 - t0, dev)
+        e_val = dist_sum(samples_per_step * ke, dev) / e_s / 1e9
+        outputs_per_step = 1.0 / int(info.n_blocks)
+        e2e = {"value": round(e_val, 3), "unit": UNIT, "h2d_bytes_per_step": spec.buffer_size,
+               "d2h_bytes_per_step": int(out_bytes * outputs_per_step), "steps": ke,
+               "api": "GatedSpectrometer.__call__ -> gspec_process (pinned host blocks)"}
+        ge.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            v, cores, desc = cpu_chain_rate(spec, kind, seconds=args.cpu_seconds)
+            cpu = {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
+        except Exception as exc:  # the CPU leg never hides a GPU result
+            cpu = {"value": None, "unit": UNIT, "cores": cpu_cores(), "kind": "port", "sample": f"failed: {exc}"}
+
+    gs.close()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": spec.name, "fft_length": spec.fft_length, "naccumulate": spec.naccumulate,
+                       "nbits": spec.nbits, "pols": spec.npol, "samples_per_pol_per_block": spec.samples_per_pol,
+                       "block_bytes": spec.buffer_size, "form": "fp32",
+                       "l2": "inputs larger than L2: two distinct blocks of %d B alternate" % spec.buffer_size,
+                       "parallelism": f"replicas x{ws} (one independent stream per GPU)"},
+            "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "roofline": roofline,
+            "cpu_baseline": cpu,
+        }
+        if lat:
+            line["latency_ms"] = {"p50": round(float(np.percentile(lat, 50)), 3),
+                                  "p95": round(float(np.percentile(lat, 95)), 3),
+                                  "p99": round(float(np.percentile(lat, 99)), 3),
+                                  "what": "host time of one handler call (H2D of the block, launch of the chain, "
+                                          "output D2H issue)"}
+        print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------- reference arm
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import gspec_cpu
+    from psrdada_cpp_gb300 import synth
+    spec, kind = workload(args.workload)
+    sub = sample_spec(spec, 1)
+    cores = cpu_cores()
+    chain = gspec_cpu.CpuChain(sub, nthreads=cores)
+    blocks = [synth.make_block(sub, seed=1, block_index=i, kind=kind) for i in range(2)]
+    for i in range(args.warmup):
+        chain.zero()
+        chain.run_block(blocks[i % 2])
+    times = []
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        c0 = time.perf_counter()
+        chain.zero()
+        chain.run_block(blocks[i % 2])
+        times.append(time.perf_counter() - c0)
+        if time.perf_counter() - t0 > args.ref_budget_s:
+            break
+    dt = time.perf_counter() - t0
+    k = len(times)
+    samples = k * sub.samples_per_pol * sub.npol
+    v = samples / dt / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": ws, "steps": k,
+        "warmup": args.warmup, "ms_per_step": round(dt / k * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": spec.name, "fft_length": spec.fft_length, "naccumulate": spec.naccumulate,
+                   "nbits": spec.nbits, "pols": spec.npol, "form": "fp32",
+                   "step": f"one output spectrum of input ({sub.samples_per_pol} samples/pol)"},
+        "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{k} steps of {sub.samples_per_pol} samples/pol of {spec.name}; the C/OpenMP "
+                                   f"restatement of the chain (the reference's own path is CUDA-only)"},
+        "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    if k < args.steps:
+        line["steps_requested"] = args.steps
+    print(json.dumps(line), flush=True)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=["c1", "c2", "c3"], default="c2")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-budget-s", type=float, default=150.0)
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

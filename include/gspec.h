@@ -77,7 +77,16 @@ typedef struct gspec_info {
   uint64_t device_bytes;          /* device memory held by the handle */
   uint64_t fft_path;              /* 0 shared-memory FFT, 1 four-step FFT */
   uint64_t n1, n2;                /* four-step split (0 for the shared-memory path) */
+  uint64_t kernel_launches;       /* kernels this handle has launched so far */
 } gspec_info;
+
+/* Per-kernel launch counts and device time (profiling enabled). */
+typedef struct gspec_kernel_profile {
+  char name[32];
+  uint64_t launches;
+  uint64_t timed_launches;
+  double total_ms;
+} gspec_kernel_profile;
 
 /* Output of one gspec_process call: when ready != 0 the handler must be
  * called with (data, size) before the next gspec_process call. */
@@ -121,6 +130,14 @@ int gspec_process_device(gspec_handle* h, const void* d_block, size_t used_bytes
 int gspec_run_block_device(gspec_handle* h, const void* d_block, void* d_out, void* cuda_stream);
 
 int gspec_get_info(const gspec_handle* h, gspec_info* info);
+
+/* Kernel accounting (new in this library; no counterpart in the reference):
+ * with profiling enabled every kernel launch is bracketed by CUDA events on
+ * its stream.  gspec_get_profile synchronises the device and returns the
+ * number of entries written; gspec_reset_profile clears the counters. */
+int gspec_set_profiling(gspec_handle* h, int enable);
+int gspec_get_profile(gspec_handle* h, gspec_kernel_profile* out, int max_entries);
+int gspec_reset_profile(gspec_handle* h);
 const char* gspec_last_error(const gspec_handle* h);
 
 /* Baselines [npol][G0, G1] currently used for the next block (device copy

@@ -561,14 +561,38 @@ class OracleSpectrometer:
 # --------------------------------------------------------------------------
 # tolerance helper shared by the parity tests
 # --------------------------------------------------------------------------
-def rel_err(got: np.ndarray, ref: np.ndarray, floor_frac: float = 1e-3) -> float:
-    """max |got-ref| / max(|ref|, floor_frac * max|ref| of that spectrum).
+def rel_err(got: np.ndarray, ref: np.ndarray, floor_frac: float = 1e-6) -> float:
+    """Maximum relative spectral error against the FP64 reference.
 
-    Spectra are compared along the last axis; the floor keeps near-zero bins
-    of signed products (Stokes U/V, Q) from dominating."""
+    Power spectra ([n_out, gate, C]): |got - ref| / |ref| per bin.
+    Stokes spectra ([n_out, IQUV, gate, C]): every product is normalised by
+    the total intensity I of the same bin (|Q|, |U|, |V| <= I), so signed
+    products near zero are measured on the scale their FP32 error lives on.
+    Denominators are floored at floor_frac times the spectrum's peak so
+    empty bins and empty gates do not divide by zero."""
     got = np.asarray(got, np.float64)
     ref = np.asarray(ref, np.float64)
-    scale = np.max(np.abs(ref), axis=-1, keepdims=True)
-    denom = np.maximum(np.abs(ref), floor_frac * scale)
+    if ref.ndim == 4:
+        base = np.abs(ref[:, 0:1])
+    else:
+        base = np.abs(ref)
+    peak = np.max(base, axis=-1, keepdims=True)
+    denom = np.maximum(base, floor_frac * peak)
     denom = np.where(denom == 0, 1.0, denom)
     return float(np.max(np.abs(got - ref) / denom))
+
+
+def rel_err_by_product(got: np.ndarray, ref: np.ndarray, floor_frac: float = 1e-6) -> dict:
+    """:func:`rel_err` per Stokes product (I, Q, U, V) or per gate (power)."""
+    if np.asarray(ref).ndim == 4:
+        out = {}
+        for i, name in enumerate("IQUV"):
+            g = np.array(got, np.float64, copy=True)
+            r = np.array(ref, np.float64, copy=True)
+            mask = np.zeros(4, bool)
+            mask[i] = True
+            g[:, ~mask] = r[:, ~mask]
+            out[name] = rel_err(g, r, floor_frac)
+        return out
+    return {f"G{g}": rel_err(np.asarray(got)[:, g:g + 1], np.asarray(ref)[:, g:g + 1], floor_frac)
+            for g in range(np.asarray(ref).shape[1])}

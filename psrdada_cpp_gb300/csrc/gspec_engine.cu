@@ -19,6 +19,8 @@
 
 using namespace gspec;
 
+constexpr int kKernelKinds = 5;
+
 struct gspec_handle {
   gspec_config cfg{};
   // layout (edd/src/DadaBufferLayout.cpp:17-39)
@@ -53,6 +55,17 @@ struct gspec_handle {
   cudaEvent_t ev_h2d[2] = {}, ev_in_free[2] = {}, ev_out_ready[2] = {};
   int ia = 1, oa = 0, ha = 0, handed = -1;
   bool host_written[2] = {false, false};
+  // launch accounting and optional per-kernel event timing
+  uint64_t launches = 0;
+  uint64_t kind_launches[kKernelKinds] = {};
+  int profiling = 0;
+  struct Pending {
+    int kind;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pending> pending;
+  double kind_ms[kKernelKinds] = {};
+  uint64_t kind_timed[kKernelKinds] = {};
   uint64_t call_count = 0;
   uint64_t device_bytes = 0;
 };
@@ -181,6 +194,26 @@ GateParams gate_params(const gspec_handle* h, const uint8_t* block) {
   return g;
 }
 
+const char* const kKernelNames[kKernelKinds] = {"small_chain", "reduce_partials", "fourstep_a", "fourstep_b",
+                                                "finalize"};
+
+// Launches one kernel of the chain; with profiling on, brackets it with
+// events on its own stream so per-kernel device time can be read back.
+template <typename F>
+cudaError_t timed(gspec_handle* h, int kind, cudaStream_t s, F&& launch) {
+  ++h->launches;
+  ++h->kind_launches[kind];
+  if (!h->profiling) return launch();
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  cudaEventRecord(a, s);
+  cudaError_t e = launch();
+  cudaEventRecord(b, s);
+  h->pending.push_back({kind, a, b});
+  return e;
+}
+
 cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out, unsigned long long* d_sat,
                          cudaStream_t s) {
   ChainParams p{};
@@ -199,10 +232,10 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
   const int N = static_cast<int>(h->cfg.fft_length);
   cudaError_t e;
   if (h->path == 0) {
-    e = launch_small_chain(N, h->cfg.nbits, h->dual, p, s);
+    e = timed(h, 0, s, [&] { return launch_small_chain(N, h->cfg.nbits, h->dual, p, s); });
     if (e != cudaSuccess) return e;
     if (h->slices > 1) {
-      e = launch_reduce_partials(N, h->dual, p, s);
+      e = timed(h, 1, s, [&] { return launch_reduce_partials(N, h->dual, p, s); });
       if (e != cudaSuccess) return e;
     }
   } else {
@@ -221,14 +254,16 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
       f.nframes = static_cast<uint32_t>(nk * h->nacc);
       f.k0 = static_cast<uint32_t>(k0);
       f.nk = static_cast<uint32_t>(nk);
-      e = launch_fourstep(N, h->cfg.nbits, h->dual, f, 0, s);
+      e = timed(h, 2, s, [&] { return launch_fourstep(N, h->cfg.nbits, h->dual, f, 0, s); });
       if (e != cudaSuccess) return e;
-      e = launch_fourstep(N, h->cfg.nbits, h->dual, f, 1, s);
+      e = timed(h, 3, s, [&] { return launch_fourstep(N, h->cfg.nbits, h->dual, f, 1, s); });
       if (e != cudaSuccess) return e;
     }
   }
-  return launch_finalize(p, h->npol, static_cast<int>(h->C), h->dual ? 1 : 0, static_cast<int>(h->cfg.convention),
-                         h->d_baselines, s);
+  return timed(h, 4, s, [&] {
+    return launch_finalize(p, h->npol, static_cast<int>(h->C), h->dual ? 1 : 0, static_cast<int>(h->cfg.convention),
+                           h->d_baselines, s);
+  });
 }
 
 uint64_t env_u64(const char* name, uint64_t dflt) {
@@ -239,6 +274,11 @@ uint64_t env_u64(const char* name, uint64_t dflt) {
 
 void release(gspec_handle* h) {
   if (!h) return;
+  for (auto& p : h->pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  h->pending.clear();
   for (int i = 0; i < 2; ++i) {
     if (h->d_in[i]) cudaFree(h->d_in[i]);
     if (h->d_out[i]) cudaFree(h->d_out[i]);
@@ -496,10 +536,54 @@ int gspec_get_info(const gspec_handle* h, gspec_info* info) {
   info->fft_path = static_cast<uint64_t>(h->path);
   info->n1 = h->N1;
   info->n2 = h->N2;
+  info->kernel_launches = h->launches;
   return GSPEC_OK;
 }
 
 const char* gspec_last_error(const gspec_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int gspec_set_profiling(gspec_handle* h, int enable) {
+  if (!h) return GSPEC_ERR_ARG;
+  h->profiling = enable ? 1 : 0;
+  return GSPEC_OK;
+}
+
+int gspec_get_profile(gspec_handle* h, gspec_kernel_profile* out, int max_entries) {
+  if (!h || !out) return GSPEC_ERR_ARG;
+  if (!cuda_ok(h, cudaDeviceSynchronize(), "sync")) return GSPEC_ERR_CUDA;
+  for (auto& p : h->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      h->kind_ms[p.kind] += ms;
+      ++h->kind_timed[p.kind];
+    }
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  h->pending.clear();
+  int n = 0;
+  for (int k = 0; k < kKernelKinds && n < max_entries; ++k) {
+    std::snprintf(out[n].name, sizeof(out[n].name), "%s", kKernelNames[k]);
+    out[n].launches = h->kind_launches[k];
+    out[n].timed_launches = h->kind_timed[k];
+    out[n].total_ms = h->kind_ms[k];
+    ++n;
+  }
+  return n;
+}
+
+int gspec_reset_profile(gspec_handle* h) {
+  if (!h) return GSPEC_ERR_ARG;
+  gspec_kernel_profile tmp[kKernelKinds];
+  gspec_get_profile(h, tmp, kKernelKinds);
+  for (int k = 0; k < kKernelKinds; ++k) {
+    h->kind_launches[k] = 0;
+    h->kind_timed[k] = 0;
+    h->kind_ms[k] = 0.0;
+  }
+  h->launches = 0;
+  return GSPEC_OK;
+}
 
 int gspec_get_baselines(gspec_handle* h, float* out4) {
   if (!h || !out4) return GSPEC_ERR_ARG;

@@ -52,7 +52,12 @@ class GspecConfig(ctypes.Structure):
 class GspecInfo(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in (
         "nchans", "n_out", "n_blocks", "nsamps_per_pol", "batch", "output_bytes", "record_bytes",
-        "device_bytes", "fft_path", "n1", "n2")]
+        "device_bytes", "fft_path", "n1", "n2", "kernel_launches")]
+
+
+class GspecKernelProfile(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 32), ("launches", ctypes.c_uint64), ("timed_launches", ctypes.c_uint64),
+                ("total_ms", ctypes.c_double)]
 
 
 class GspecOutput(ctypes.Structure):
@@ -86,6 +91,9 @@ def load_library() -> ctypes.CDLL:
     lib.gspec_set_baselines.argtypes = [vp, ctypes.POINTER(ctypes.c_float)]
     lib.gspec_get_saturation.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
     lib.gspec_unpack_device.argtypes = [vp, u32, u64, vp, vp]
+    lib.gspec_set_profiling.argtypes = [vp, ctypes.c_int]
+    lib.gspec_get_profile.argtypes = [vp, ctypes.POINTER(GspecKernelProfile), ctypes.c_int]
+    lib.gspec_reset_profile.argtypes = [vp]
     lib.gspec_gate_device.argtypes = [vp, vp, vp, vp]
     _LIB = lib
     return lib
@@ -305,6 +313,18 @@ class GatedSpectrometer:
     def gate_device(self, d_block: int, d_gated: int, stream: int = 0) -> None:
         self._check(self._lib.gspec_gate_device(self._h, ctypes.c_void_p(d_block), ctypes.c_void_p(d_gated),
                                                 ctypes.c_void_p(stream)))
+
+    def set_profiling(self, enable: bool) -> None:
+        self._check(self._lib.gspec_set_profiling(self._h, 1 if enable else 0))
+
+    def profile(self) -> dict:
+        """{kernel name: (launches, timed launches, total device ms)}."""
+        arr = (GspecKernelProfile * 8)()
+        n = self._check(self._lib.gspec_get_profile(self._h, arr, 8))
+        return {arr[i].name.decode(): (arr[i].launches, arr[i].timed_launches, arr[i].total_ms) for i in range(n)}
+
+    def reset_profile(self) -> None:
+        self._check(self._lib.gspec_reset_profile(self._h))
 
     def last_error(self) -> str:
         return self._lib.gspec_last_error(self._h).decode()
