@@ -251,6 +251,8 @@ struct GateParams {
   uint32_t chunk;            // samples per gating chunk (reference)
   uint32_t step;             // items per gating chunk (reference)
   uint32_t nbits;
+  int32_t heap_shift;        // intended convention: log2(samples per heap) when that is an integer power of 2, else -1
+  const uint8_t* masks;      // per item index: bit0 = gate 0 (m0), bit1 = gate 1 (m1); built by the mask pass
 };
 
 __device__ __forceinline__ uint32_t item_index(const GateParams& g, uint32_t s) {
@@ -259,6 +261,7 @@ __device__ __forceinline__ uint32_t item_index(const GateParams& g, uint32_t s) 
     const uint32_t t = s - j * g.chunk;
     return j * g.step + (t / g.heap_size) * g.nsc + g.sel;
   }
+  if (g.heap_shift >= 0) return (s >> g.heap_shift) * g.nsc + g.sel;
   const uint64_t bit = static_cast<uint64_t>(s) * g.nbits;
   return static_cast<uint32_t>(bit / (8ull * g.heap_size)) * g.nsc + g.sel;
 }
@@ -270,16 +273,14 @@ __device__ __forceinline__ const uint8_t* pol_byte(const GateParams& g, int pol,
   return g.block + (2 * h + pol) * g.heap_size + (b - h * g.heap_size);
 }
 
-// Selected item of one pol after the dual-pol merge
-// (edd/src/GatedSpectrometer.cu:9-19 logical OR in the reference convention,
-// bitwise OR in the intended one).
-__device__ __forceinline__ uint64_t load_item(const GateParams& g, int pol, uint32_t idx) {
+// Selected item after the dual-pol merge (edd/src/GatedSpectrometer.cu:9-19:
+// logical OR in the reference convention, bitwise OR in the intended one).
+__device__ __forceinline__ uint64_t load_item(const GateParams& g, uint32_t idx) {
   const uint64_t* items = reinterpret_cast<const uint64_t*>(g.block + g.sc_offset);
   if (!g.dual) return __ldg(items + idx);
   const uint64_t a = __ldg(items + 2ull * idx);
   const uint64_t b = __ldg(items + 2ull * idx + 1);
   if (g.convention == 1) return (a != 0 || b != 0) ? 1ull : 0ull;
-  (void)pol;
   return a | b;
 }
 
@@ -297,12 +298,21 @@ struct GateStats {
   long long s0 = 0, s1 = 0;
 };
 
+// Gate masks of an item index from the mask pass.
+__device__ __forceinline__ void mask_of(const GateParams& g, uint32_t idx, bool& m0, bool& m1) {
+  const uint32_t m = __ldg(g.masks + idx);
+  m0 = m & 1u;
+  m1 = (m >> 1) & 1u;
+}
+
 // Unpack + gate one group of samples of one pol starting at pol sample s.
-// Writes gated G0/G1 floats into g0[], g1[] and updates the statistics.
+// Writes gated G0/G1 floats into g0[], g1[]; adds the statistics of gate 0
+// when (stat_gates & 1) and of gate 1 when (stat_gates & 2), so that a
+// sample visited by two jobs is counted once.
 template <int NBITS>
 __device__ __forceinline__ void gate_group(const GateParams& g, int pol, uint32_t s, float b0, float b1,
                                            float (&g0)[Group<NBITS>::samples], float (&g1)[Group<NBITS>::samples],
-                                           GateStats& st) {
+                                           GateStats& st, uint32_t stat_gates = 3u) {
   constexpr int GS = Group<NBITS>::samples;
   int v[GS];
   const uint64_t byte0 = static_cast<uint64_t>(s) * NBITS / 8;
@@ -310,16 +320,40 @@ __device__ __forceinline__ void gate_group(const GateParams& g, int pol, uint32_
   const uint32_t ia = item_index(g, s);
   const uint32_t ib = item_index(g, s + GS - 1);
   bool a0, a1;
-  item_masks(load_item(g, pol, ia), g.bitpos, a0, a1);
+  mask_of(g, ia, a0, a1);
   bool c0 = a0, c1 = a1;
   uint32_t boundary = 0xffffffffu;
   if (ib != ia) {
-    item_masks(load_item(g, pol, ib), g.bitpos, c0, c1);
+    mask_of(g, ib, c0, c1);
     // first sample whose item is ib
     boundary = s;
     while (boundary < s + GS && item_index(g, boundary) == ia) ++boundary;
   }
+  const bool k0 = stat_gates & 1u, k1 = stat_gates & 2u;
   constexpr int lo = -(1 << (NBITS - 1)), hi = (1 << (NBITS - 1)) - 1;
+  if (ib == ia) {
+    // the whole group lies in one heap: statistics per group
+    int sumv = 0, satc = 0;
+#pragma unroll
+    for (int i = 0; i < GS; ++i) {
+      const float vf = static_cast<float>(v[i]);
+      g0[i] = gate_value(vf, b0, a0);
+      g1[i] = gate_value(vf, b1, a1);
+      sumv += v[i];
+      satc += (v[i] == lo) | (v[i] == hi);
+    }
+    if (a0 && k0) {
+      st.n0 += GS;
+      st.s0 += sumv;
+      st.sat0 += satc;
+    }
+    if (a1 && k1) {
+      st.n1 += GS;
+      st.s1 += sumv;
+      st.sat1 += satc;
+    }
+    return;
+  }
 #pragma unroll
   for (int i = 0; i < GS; ++i) {
     const bool second = (s + i) >= boundary;
@@ -329,13 +363,118 @@ __device__ __forceinline__ void gate_group(const GateParams& g, int pol, uint32_
     g0[i] = gate_value(vf, b0, m0);
     g1[i] = gate_value(vf, b1, m1);
     const bool sat = (v[i] == lo) | (v[i] == hi);
-    st.n0 += m0;
-    st.n1 += m1;
-    st.sat0 += (m0 && sat);
-    st.sat1 += (m1 && sat);
-    st.s0 += m0 ? v[i] : 0;
-    st.s1 += m1 ? v[i] : 0;
+    const bool q0 = m0 && k0, q1 = m1 && k1;
+    st.n0 += q0;
+    st.n1 += q1;
+    st.sat0 += (q0 && sat);
+    st.sat1 += (q1 && sat);
+    st.s0 += q0 ? v[i] : 0;
+    st.s1 += q1 ? v[i] : 0;
   }
+}
+
+// One gate of one group: out[] = gate `gate` of the samples; statistics of
+// that gate only when `stats` is set.
+template <int NBITS>
+__device__ __forceinline__ void gate_group1(const GateParams& g, int pol, uint32_t s, float b, int gate,
+                                            float (&out)[Group<NBITS>::samples], GateStats& st, bool stats) {
+  constexpr int GS = Group<NBITS>::samples;
+  int v[GS];
+  const uint64_t byte0 = static_cast<uint64_t>(s) * NBITS / 8;
+  unpack_group<NBITS>(pol_byte(g, pol, byte0), v);
+  const uint32_t ia = item_index(g, s);
+  const uint32_t ib = item_index(g, s + GS - 1);
+  const uint32_t sh = gate ? 1u : 0u;
+  const bool ma = (__ldg(g.masks + ia) >> sh) & 1u;
+  constexpr int lo = -(1 << (NBITS - 1)), hi = (1 << (NBITS - 1)) - 1;
+  int sumv = 0, satc = 0, cnt = 0;
+  if (ib == ia) {
+#pragma unroll
+    for (int i = 0; i < GS; ++i) {
+      out[i] = gate_value(static_cast<float>(v[i]), b, ma);
+      sumv += v[i];
+      satc += (v[i] == lo) | (v[i] == hi);
+    }
+    cnt = ma ? GS : 0;
+    if (!ma) sumv = satc = 0;
+  } else {
+    const bool mb = (__ldg(g.masks + ib) >> sh) & 1u;
+    uint32_t boundary = s;
+    while (boundary < s + GS && item_index(g, boundary) == ia) ++boundary;
+#pragma unroll
+    for (int i = 0; i < GS; ++i) {
+      const bool m = (s + i) >= boundary ? mb : ma;
+      out[i] = gate_value(static_cast<float>(v[i]), b, m);
+      cnt += m;
+      sumv += m ? v[i] : 0;
+      satc += m && ((v[i] == lo) | (v[i] == hi));
+    }
+  }
+  if (stats) {
+    if (gate) {
+      st.n1 += cnt;
+      st.s1 += sumv;
+      st.sat1 += satc;
+    } else {
+      st.n0 += cnt;
+      st.s0 += sumv;
+      st.sat0 += satc;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ jobs
+// A job is one complex FFT of two real sequences packed as z = a + i b.
+//   single pol: a = gate gA of frame fA, b = gate gB of frame fB (or zero);
+//               a frame with data in both gates is one job (f,0)+(f,1),
+//               frames with data in one gate are paired two per job;
+//   dual pol:   a = pol 0, b = pol 1 of gate gA of frame fA.
+// Gates without any sample in a frame are constant (their baseline) and
+// contribute only to bin 0, counted in dc[gate].
+// Encoding: fA | gA << 14 | fB << 16 | gB << 30, fB == kNoFrame: no b.
+constexpr uint32_t kNoFrame = 0x3FFFu;
+constexpr uint32_t kMaxJobFrames = 0x3FFFu;
+
+__host__ __device__ __forceinline__ uint32_t job_pack(uint32_t fa, uint32_t ga, uint32_t fb, uint32_t gb) {
+  return fa | (ga << 14) | (fb << 16) | (gb << 30);
+}
+__device__ __forceinline__ uint32_t job_fa(uint32_t j) { return j & 0x3FFFu; }
+__device__ __forceinline__ uint32_t job_ga(uint32_t j) { return (j >> 14) & 1u; }
+__device__ __forceinline__ uint32_t job_fb(uint32_t j) { return (j >> 16) & 0x3FFFu; }
+__device__ __forceinline__ uint32_t job_gb(uint32_t j) { return (j >> 30) & 1u; }
+
+// Builds the job list of nf frames whose gate flags (bit0 gate 0 has data,
+// bit1 gate 1 has data) are flags[0..nf); frame numbers in the jobs are
+// relative to flags.  Returns the number of jobs; dc[g] receives the number
+// of frames whose gate g holds no data.  Run by one thread.
+__device__ __forceinline__ uint32_t build_jobs(const uint8_t* flags, uint32_t nf, bool dual, uint32_t* jobs,
+                                               uint32_t (&dc)[2]) {
+  uint32_t n = 0;
+  dc[0] = dc[1] = 0;
+  uint32_t pend = kNoFrame, pend_g = 0;
+  for (uint32_t f = 0; f < nf; ++f) {
+    const uint32_t fl = flags[f];
+    const bool a0 = fl & 1u, a1 = fl & 2u;
+    dc[0] += !a0;
+    dc[1] += !a1;
+    if (dual) {
+      if (a0) jobs[n++] = job_pack(f, 0, kNoFrame, 0);
+      if (a1) jobs[n++] = job_pack(f, 1, kNoFrame, 0);
+    } else if (a0 && a1) {
+      jobs[n++] = job_pack(f, 0, f, 1);
+    } else if (a0 || a1) {
+      const uint32_t gsel = a1 ? 1u : 0u;
+      if (pend == kNoFrame) {
+        pend = f;
+        pend_g = gsel;
+      } else {
+        jobs[n++] = job_pack(pend, pend_g, f, gsel);
+        pend = kNoFrame;
+      }
+    }
+  }
+  if (pend != kNoFrame) jobs[n++] = job_pack(pend, pend_g, kNoFrame, 0);
+  return n;
 }
 
 }  // namespace gspec

@@ -19,7 +19,7 @@
 
 using namespace gspec;
 
-constexpr int kKernelKinds = 5;
+constexpr int kKernelKinds = 8;
 
 struct gspec_handle {
   gspec_config cfg{};
@@ -51,6 +51,13 @@ struct gspec_handle {
   float2* d_twB = nullptr;
   float* d_partial = nullptr;
   float2* d_scratch = nullptr;
+  uint8_t* d_masks = nullptr;      // per side-channel item index: gates
+  uint8_t* d_flags = nullptr;      // per frame: gates holding data
+  uint32_t* d_jobs = nullptr;      // four-step job lists [kchunk][maxjobs]
+  uint32_t* d_njobs = nullptr;
+  uint32_t* d_dc = nullptr;
+  uint32_t maxjobs = 0;
+  int32_t heap_shift = -1;
   cudaStream_t h2d = nullptr, proc = nullptr, d2h = nullptr;
   cudaEvent_t ev_h2d[2] = {}, ev_in_free[2] = {}, ev_out_ready[2] = {};
   int ia = 1, oa = 0, ha = 0, handed = -1;
@@ -148,6 +155,16 @@ bool configure(gspec_handle* h) {
     return fail("dual-pol heap size must be a multiple of " + std::to_string(gb) + " bytes");
   }
   if (c.heap_size < static_cast<uint64_t>(gb)) return fail("heap smaller than one unpack group");
+  // samples per heap as a shift when it is an integer power of two
+  h->heap_shift = -1;
+  if ((8 * c.heap_size) % c.nbits == 0) {
+    const uint64_t sph = 8 * c.heap_size / c.nbits;
+    if ((sph & (sph - 1)) == 0) {
+      int sh = 0;
+      while ((1ull << sh) < sph) ++sh;
+      h->heap_shift = sh;
+    }
+  }
   // edd/detail/GatedSpectrometer.cu:114-130
   const uint64_t per_out = N * c.naccumulate;
   if (per_out <= h->nsamps) {
@@ -191,11 +208,13 @@ GateParams gate_params(const gspec_handle* h, const uint8_t* block) {
   g.chunk = static_cast<uint32_t>(h->nsamps / h->n_out);
   g.step = static_cast<uint32_t>(h->items_per_pol / h->n_out);
   g.nbits = h->cfg.nbits;
+  g.heap_shift = h->heap_shift;
+  g.masks = h->d_masks;
   return g;
 }
 
-const char* const kKernelNames[kKernelKinds] = {"small_chain", "reduce_partials", "fourstep_a", "fourstep_b",
-                                                "finalize"};
+const char* const kKernelNames[kKernelKinds] = {"small_chain", "reduce_finalize", "fourstep_a", "fourstep_b",
+                                                "finalize",    "gate_prepass",    "unused",     "fourstep_plan"};
 
 // Launches one kernel of the chain; with profiling on, brackets it with
 // events on its own stream so per-kernel device time can be read back.
@@ -229,14 +248,24 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
   p.nacc = static_cast<uint32_t>(h->nacc);
   p.slices = h->slices;
   p.frames_per_unit = h->frames_per_unit;
+  p.flags = h->d_flags;
   const int N = static_cast<int>(h->cfg.fft_length);
   cudaError_t e;
+  // gate masks per item and the gates each frame holds data in
+  e = timed(h, 5, s, [&] {
+    return launch_prepass(p.g, static_cast<uint32_t>(h->items_per_pol), h->d_masks, static_cast<uint32_t>(N),
+                          static_cast<uint32_t>(h->batch), h->d_flags, s);
+  });
+  if (e != cudaSuccess) return e;
   if (h->path == 0) {
     e = timed(h, 0, s, [&] { return launch_small_chain(N, h->cfg.nbits, h->dual, p, s); });
     if (e != cudaSuccess) return e;
     if (h->slices > 1) {
-      e = timed(h, 1, s, [&] { return launch_reduce_partials(N, h->dual, p, s); });
-      if (e != cudaSuccess) return e;
+      // partial spectra of the slices, then the baselines of the next block
+      return timed(h, 1, s, [&] {
+        return launch_reduce_finalize(N, h->dual, p, h->npol, static_cast<int>(h->cfg.convention), h->d_baselines,
+                                      s);
+      });
     }
   } else {
     FourStepParams f{};
@@ -248,10 +277,17 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
     f.twB = h->d_twB;
     f.N1 = h->N1;
     f.N2 = h->N2;
+    f.maxjobs = h->maxjobs;
+    f.jobs = h->d_jobs;
+    f.njobs = h->d_njobs;
+    f.dc = h->d_dc;
+    // job lists of every output spectrum of the block
+    f.k0 = 0;
+    f.nk = static_cast<uint32_t>(h->n_out);
+    e = timed(h, 7, s, [&] { return launch_fourstep(N, h->cfg.nbits, h->dual, f, -1, s); });
+    if (e != cudaSuccess) return e;
     for (uint64_t k0 = 0; k0 < h->n_out; k0 += h->kchunk) {
       const uint64_t nk = std::min<uint64_t>(h->kchunk, h->n_out - k0);
-      f.frame0 = static_cast<uint32_t>(k0 * h->nacc);
-      f.nframes = static_cast<uint32_t>(nk * h->nacc);
       f.k0 = static_cast<uint32_t>(k0);
       f.nk = static_cast<uint32_t>(nk);
       e = timed(h, 2, s, [&] { return launch_fourstep(N, h->cfg.nbits, h->dual, f, 0, s); });
@@ -288,8 +324,9 @@ void release(gspec_handle* h) {
     if (h->ev_in_free[i]) cudaEventDestroy(h->ev_in_free[i]);
     if (h->ev_out_ready[i]) cudaEventDestroy(h->ev_out_ready[i]);
   }
-  void* ptrs[] = {h->d_sat_dev, h->d_baselines, h->d_pol_stats, h->d_tw, h->d_tw1, h->d_tw2,
-                  h->d_twA,     h->d_twB,       h->d_partial,   h->d_scratch};
+  void* ptrs[] = {h->d_sat_dev, h->d_baselines, h->d_pol_stats, h->d_tw,   h->d_tw1,   h->d_tw2,  h->d_twA,
+                  h->d_twB,     h->d_partial,   h->d_scratch,   h->d_masks, h->d_flags, h->d_jobs, h->d_njobs,
+                  h->d_dc};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->h2d) cudaStreamDestroy(h->h2d);
@@ -414,17 +451,24 @@ gspec_handle* gspec_create(const gspec_config* cfg, char* err, size_t err_len) {
       s = 1;
       while (h->n_out * s < target && h->nacc % (2 * s) == 0) s *= 2;
     }
+    while (h->nacc / s > kMaxUnitFrames && h->nacc % (2 * s) == 0) s *= 2;
     if (h->nacc % s) return bail("GSPEC_SLICES must divide the frames per output spectrum");
+    if (h->nacc / s > kMaxUnitFrames) return bail("more than 1024 frames per work unit");
     h->slices = static_cast<uint32_t>(s);
     h->frames_per_unit = static_cast<uint32_t>(h->nacc / s);
   } else {
-    const uint64_t budget = env_u64("GSPEC_SCRATCH_MB", 512) << 20;
-    const uint64_t per_out = h->nacc * (h->dual ? 2 : 1) * static_cast<uint64_t>(N) * sizeof(float2);
+    if (h->nacc > kMaxJobFrames) return bail("more than 16383 frames per output spectrum in one block");
+    h->maxjobs = static_cast<uint32_t>(h->nacc * (h->dual ? 2 : 1));
+    // scratch of the chunk of output spectra in flight (kept near L2 size)
+    const uint64_t budget = env_u64("GSPEC_SCRATCH_MB", 256) << 20;
+    const uint64_t per_out = static_cast<uint64_t>(h->maxjobs) * static_cast<uint64_t>(N) * sizeof(float2);
     uint64_t kc = budget / per_out;
     if (kc < 1) kc = 1;
     if (kc > h->n_out) kc = h->n_out;
     h->kchunk = static_cast<uint32_t>(kc);
   }
+  if (!dalloc(h, &h->d_masks, h->items_per_pol, "gate masks") || !dalloc(h, &h->d_flags, h->batch, "frame flags"))
+    return bail("");
   for (int i = 0; i < 2; ++i) {
     if (!dalloc(h, &h->d_in[i], cfg->buffer_size, "input") || !dalloc(h, &h->d_out[i], h->out_bytes, "output") ||
         !dalloc(h, &h->d_sat[i], h->ext_bytes, "saturation"))
@@ -459,9 +503,11 @@ gspec_handle* gspec_create(const gspec_config* cfg, char* err, size_t err_len) {
         !cuda_ok(h, launch_twiddles(h->N2, h->d_tw2, h->proc), "twiddles") ||
         !cuda_ok(h, launch_fourstep_twiddles(N, h->d_twA, h->d_twB, h->proc), "twiddles"))
       return bail("");
-    const uint64_t frames = static_cast<uint64_t>(h->kchunk) * h->nacc;
-    if (!dalloc(h, &h->d_scratch, frames * (h->dual ? 2 : 1) * static_cast<uint64_t>(N) * sizeof(float2),
-                "four-step scratch"))
+    const uint64_t slots = static_cast<uint64_t>(h->kchunk) * h->maxjobs;
+    if (!dalloc(h, &h->d_scratch, slots * static_cast<uint64_t>(N) * sizeof(float2), "four-step scratch") ||
+        !dalloc(h, &h->d_jobs, h->n_out * h->maxjobs * sizeof(uint32_t), "job lists") ||
+        !dalloc(h, &h->d_njobs, h->n_out * sizeof(uint32_t), "job counts") ||
+        !dalloc(h, &h->d_dc, 2ull * h->n_out * sizeof(uint32_t), "dc counts"))
       return bail("");
   }
   if (!cuda_ok(h, cudaStreamSynchronize(h->proc), "setup")) return bail("");
@@ -621,8 +667,11 @@ int gspec_gate_device(gspec_handle* h, const void* d_block, float* d_gated, void
   if (!h || !d_block || !d_gated) return GSPEC_ERR_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
   if (!cuda_ok(h, cudaStreamSynchronize(h->proc), "sync")) return GSPEC_ERR_CUDA;
-  if (!cuda_ok(h, launch_gate_debug(h->cfg.nbits, gate_params(h, static_cast<const uint8_t*>(d_block)),
-                                    h->d_baselines, h->npol, static_cast<uint32_t>(h->nsamps), d_gated, s),
+  const GateParams g = gate_params(h, static_cast<const uint8_t*>(d_block));
+  if (!cuda_ok(h, launch_prepass(g, static_cast<uint32_t>(h->items_per_pol), h->d_masks, 0, 0, nullptr, s),
+               "mask kernel") ||
+      !cuda_ok(h, launch_gate_debug(h->cfg.nbits, g, h->d_baselines, h->npol, static_cast<uint32_t>(h->nsamps),
+                                    d_gated, s),
                "gate kernel"))
     return GSPEC_ERR_CUDA;
   return GSPEC_OK;

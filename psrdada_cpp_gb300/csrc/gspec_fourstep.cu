@@ -6,11 +6,12 @@
 // Z[k1 + N1*k2].  Rows k1 and N1-k1 hold each bin's mirror N-k, so pass B
 // takes them as a pair, splits the packed real sequences and accumulates the
 // power (edd/DetectorAccumulator.cuh:40-61) or Stokes
-// (edd/src/GatedSpectrometer.cu:140-169) spectra over the frames of one
-// output spectrum before writing them once.
+// (edd/src/GatedSpectrometer.cu:140-169) spectra over the jobs of one output
+// spectrum before writing them once.
 //
-// Pass A runs once per gate: single pol packs G0 + i G1 (one sequence);
-// dual pol packs P0 + i P1 of gate 0 or gate 1 (grid dimension).
+// The plan kernel builds each output spectrum's job list (build_jobs): only
+// gates holding data are transformed; gates without data add their constant
+// baseline to bin 0.
 #include "gspec_kernels.cuh"
 
 namespace gspec {
@@ -23,8 +24,8 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
   return v;
 }
 
-// Same commit rule as the small path: per-pol n0, n1, s0, s1 to pol_stats;
-// n0, n1 summed over pols to the output record; saturation to sat[k].
+// Same commit rule as the shared-memory path: per-pol n0, n1, s0, s1 to
+// pol_stats; n0, n1 summed over pols to the output record; saturation to sat[k].
 template <int NPOL>
 __device__ void commit(const ChainParams& p, const GateStats (&st)[NPOL], uint32_t k, int vals_c,
                        unsigned long long* red) {
@@ -74,24 +75,34 @@ __device__ void commit(const ChainParams& p, const GateStats (&st)[NPOL], uint32
 
 }  // namespace
 
+// One thread per output spectrum of the launch: its job list.
+__global__ void fourstep_plan_kernel(FourStepParams p, int dual) {
+  const uint32_t kk = blockIdx.x * blockDim.x + threadIdx.x;
+  if (kk >= p.nk) return;
+  const uint32_t k = p.k0 + kk;
+  uint32_t dc[2];
+  p.njobs[k] = build_jobs(p.c.flags + k * p.c.nacc, p.c.nacc, dual != 0, p.jobs + k * p.maxjobs, dc);
+  p.dc[2 * k] = dc[0];
+  p.dc[2 * k + 1] = dc[1];
+}
+
 template <int N1>
 struct PassACfg {
   static constexpr int BC = N1 >= 1024 ? 8 : 16;     // columns per CTA
   static constexpr int T1 = N1 / 16;
   static constexpr int THREADS = BC * T1;
   static constexpr int STRIDE = spad_size(N1) + 1;  // odd: column-wise reads are conflict-free
-  static constexpr size_t RED = static_cast<size_t>(THREADS / 32) * 12 * 8;
+  static constexpr size_t RED = static_cast<size_t>(THREADS / 32 > 0 ? THREADS / 32 : 1) * 12 * 8;
   static constexpr size_t SMEM = static_cast<size_t>(BC) * STRIDE * sizeof(float2) + RED;
 };
 
-// grid.x = nframes * (N2 / BC) * ngates
+// grid.x = nk * maxjobs * (N2 / BC): (output spectrum, job, column tile)
 template <int N1, int NBITS, bool DUAL>
 __global__ void __launch_bounds__(PassACfg<N1>::THREADS) fourstep_a_kernel(FourStepParams p) {
   using Cfg = PassACfg<N1>;
   constexpr int BC = Cfg::BC;
   constexpr int G = Group<NBITS>::samples;
   constexpr int NPOL = DUAL ? 2 : 1;
-  constexpr int NGATES = DUAL ? 2 : 1;
   extern __shared__ float4 smem_f4[];
   float2* S = reinterpret_cast<float2*>(smem_f4);
   unsigned long long* red =
@@ -100,13 +111,15 @@ __global__ void __launch_bounds__(PassACfg<N1>::THREADS) fourstep_a_kernel(FourS
   const uint32_t N2 = p.N2;
   const uint32_t N = N1 * N2;
   const uint32_t tiles = N2 / BC;
-  uint32_t u = blockIdx.x;
-  const uint32_t gate = u % NGATES;
-  u /= NGATES;
-  const uint32_t tile = u % tiles;
-  const uint32_t fl = u / tiles;
-  const uint32_t f = p.frame0 + fl;
-  const uint32_t k = f / p.c.nacc;
+  const uint32_t tile = blockIdx.x % tiles;
+  const uint32_t j = (blockIdx.x / tiles) % p.maxjobs;
+  const uint32_t kk = blockIdx.x / (tiles * p.maxjobs);
+  const uint32_t k = p.k0 + kk;
+  if (j >= p.njobs[k]) return;
+  const uint32_t job = p.jobs[k * p.maxjobs + j];
+  const uint32_t fa = job_fa(job), ga = job_ga(job), fb = job_fb(job), gb = job_gb(job);
+  const uint32_t frA = k * p.c.nacc + fa;
+  const uint32_t frB = k * p.c.nacc + fb;
   const uint32_t c0 = tile * BC;
   const int tid = threadIdx.x;
 
@@ -118,33 +131,34 @@ __global__ void __launch_bounds__(PassACfg<N1>::THREADS) fourstep_a_kernel(FourS
   constexpr int GPR = G <= BC ? BC / G : 1;
   const uint32_t gbase = G <= BC ? c0 : (c0 / G) * G;
   const int keep0 = static_cast<int>(c0 - gbase);        // first kept element of a group
-  const bool count_stats = (gate == 0) && (c0 == gbase || G <= BC);
+  const bool count_stats = (c0 == gbase || G <= BC);
+  const uint32_t sg_a = count_stats ? (DUAL ? (1u << ga) : 3u) : 0u;
 
   GateStats st[NPOL];
-  GateStats junk[NPOL];
   for (int w = tid; w < N1 * GPR; w += Cfg::THREADS) {
     const int n1 = w % N1;
     const int gi = w / N1;
     const uint32_t gs = gbase + gi * G;
-    const uint32_t s = f * N + N2 * n1 + gs;
-    float a0[G], a1[G];
-    gate_group<NBITS>(p.c.g, 0, s, bl[0], bl[1], a0, a1, count_stats ? st[0] : junk[0]);
-    float b0[G], b1[G];
+    const uint32_t off = N2 * n1 + gs;
+    float re[G], im[G];
     if constexpr (DUAL) {
-      gate_group<NBITS>(p.c.g, 1, s, bl[2], bl[3], b0, b1, count_stats ? st[NPOL - 1] : junk[NPOL - 1]);
+      gate_group1<NBITS>(p.c.g, 0, frA * N + off, bl[ga], ga, re, st[0], count_stats);
+      gate_group1<NBITS>(p.c.g, 1, frA * N + off, bl[2 + ga], ga, im, st[NPOL - 1], count_stats);
+    } else if (fb == fa) {
+      gate_group<NBITS>(p.c.g, 0, frA * N + off, bl[0], bl[1], re, im, st[0], sg_a);
+    } else {
+      gate_group1<NBITS>(p.c.g, 0, frA * N + off, bl[ga], ga, re, st[0], count_stats);
+      if (fb != kNoFrame) {
+        gate_group1<NBITS>(p.c.g, 0, frB * N + off, bl[gb], gb, im, st[0], count_stats);
+      } else {
+#pragma unroll
+        for (int e = 0; e < G; ++e) im[e] = 0.f;
+      }
     }
 #pragma unroll
     for (int e = 0; e < G; ++e) {
       const int col = static_cast<int>(gs - c0) + e;
-      if (G <= BC || (e >= keep0 && e < keep0 + BC)) {
-        float2 z;
-        if constexpr (DUAL) {
-          z = gate ? make_float2(a1[e], b1[e]) : make_float2(a0[e], b0[e]);
-        } else {
-          z = make_float2(a0[e], a1[e]);
-        }
-        S[col * Cfg::STRIDE + spad(n1)] = z;
-      }
+      if (G <= BC || (e >= keep0 && e < keep0 + BC)) S[col * Cfg::STRIDE + spad(n1)] = make_float2(re[e], im[e]);
     }
   }
   __syncthreads();
@@ -154,118 +168,160 @@ __global__ void __launch_bounds__(PassACfg<N1>::THREADS) fourstep_a_kernel(FourS
     fft_smem<N1, 16>(S + sq * Cfg::STRIDE, p.tw1, t, true);
   }
   // twiddle W_N^(n2*k1) and store Y[k1][n2]
-  float2* dst = p.scratch + (static_cast<size_t>(fl) * NGATES + gate) * N;
+  float2* dst = p.scratch + (static_cast<size_t>(kk) * p.maxjobs + j) * N;
   for (int w = tid; w < BC * N1; w += Cfg::THREADS) {
     const int col = w % BC;
     const int k1 = w / BC;
-    float2 v = S[col * Cfg::STRIDE + spad(k1)];
+    const float2 v = S[col * Cfg::STRIDE + spad(k1)];
     const uint32_t m = (c0 + col) * static_cast<uint32_t>(k1);
     const float2 W = cmul(__ldg(&p.twA[m >> 10]), __ldg(&p.twB[m & 1023]));
     dst[static_cast<size_t>(k1) * N2 + c0 + col] = cmul(v, W);
   }
-  if (gate == 0) commit<NPOL>(p.c, st, k, (DUAL ? 8 : 2) * static_cast<int>(N / 2 + 1), red);
+  commit<NPOL>(p.c, st, k, (DUAL ? 8 : 2) * static_cast<int>(N / 2 + 1), red);
 }
 
 template <int N2, bool DUAL>
 struct PassBCfg {
-  static constexpr int SEQ = DUAL ? 2 : 1;
   static constexpr int T2 = N2 / 16;
-  static constexpr int THREADS = 2 * SEQ * T2;
+  static constexpr int SLOT_THREADS = 2 * T2;        // one row pair: rows rp and N1-rp
+  static constexpr int NSLOT = 256 / SLOT_THREADS;   // jobs in flight per CTA
+  static constexpr int THREADS = NSLOT * SLOT_THREADS;
   static constexpr int STRIDE = spad_size(N2);
   static constexpr int VALS = DUAL ? 8 : 2;
   static constexpr int NA = N2 + 1;                  // accumulated bins per row pair
-  static constexpr size_t SMEM =
-      static_cast<size_t>(2 * SEQ) * STRIDE * sizeof(float2) + static_cast<size_t>(VALS) * NA * sizeof(float);
+  static constexpr size_t SMEM = static_cast<size_t>(2 * NSLOT) * STRIDE * sizeof(float2) +
+                                 static_cast<size_t>(VALS) * NSLOT * NA * sizeof(float);
 };
 
-// grid.x = nk * N1/2: unit (output spectrum k, row pair rp)
+// Row pair rp holds rows rp and N1-rp (rp = 0: rows 0 and N1/2).  Accumulator
+// slot a of the pair maps to these bins:
+//   rp != 0: a < N2/2 -> row rp, k2 = a (mirror: row N1-rp, N2-1-a);
+//            a >= N2/2 -> row N1-rp, k2 = a - N2/2 (mirror: row rp, N2-1-k2)
+//   rp == 0: a <= N2/2 -> row 0, k2 = a (mirror: row 0, N2-a mod N2);
+//            a > N2/2 -> row N1/2, k2 = a-N2/2-1 (mirror: row N1/2, N2-1-k2)
+template <int N2>
+__device__ __forceinline__ void pair_slot(uint32_t rp, int a, int& r, int& k2, int& pr, int& k2p) {
+  if (rp != 0) {
+    if (a < N2 / 2) { r = 0; k2 = a; pr = 1; k2p = N2 - 1 - a; }
+    else { r = 1; k2 = a - N2 / 2; pr = 0; k2p = N2 - 1 - k2; }
+  } else {
+    if (a <= N2 / 2) { r = 0; k2 = a; pr = 0; k2p = (N2 - a) & (N2 - 1); }
+    else { r = 1; k2 = a - N2 / 2 - 1; pr = 1; k2p = N2 - 1 - k2; }
+  }
+}
+
+// grid.x = nk * N1/2: unit (output spectrum k, row pair rp).  The unit's
+// jobs are spread over NSLOT slots (job j in slot j % NSLOT); every slot
+// accumulates in its own shared-memory spectrum and the slots are summed in
+// a fixed order at the end.
 template <int N2, bool DUAL>
-__global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS) fourstep_b_kernel(FourStepParams p) {
+__global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, 2) fourstep_b_kernel(FourStepParams p) {
   using Cfg = PassBCfg<N2, DUAL>;
-  constexpr int SEQ = Cfg::SEQ;
   constexpr int NA = Cfg::NA;
+  constexpr int VA = Cfg::VALS * NA;
   extern __shared__ float4 smem_f4[];
-  float2* S = reinterpret_cast<float2*>(smem_f4);      // [row r][seq] sequences
-  float* acc = reinterpret_cast<float*>(S + 2 * SEQ * Cfg::STRIDE);
+  float2* S = reinterpret_cast<float2*>(smem_f4);                    // [slot][row r] sequences
+  float* acc = reinterpret_cast<float*>(S + 2 * Cfg::NSLOT * Cfg::STRIDE);   // [slot][v][a]
 
   const uint32_t N1 = p.N1;
   const uint32_t N = N1 * N2;
   const uint32_t C = N / 2 + 1;
   const uint32_t half = N1 / 2;
-  const uint32_t k = p.k0 + blockIdx.x / half;
+  const uint32_t kk = blockIdx.x / half;
+  const uint32_t k = p.k0 + kk;
   const uint32_t rp = blockIdx.x % half;
-  const uint32_t rowA = rp;
-  const uint32_t rowB = rp == 0 ? half : N1 - rp;
-  const int tid = threadIdx.x;
-
-  for (int i = tid; i < Cfg::VALS * NA; i += Cfg::THREADS) acc[i] = 0.f;
-
+  const uint32_t rowA = rp, rowB = rp == 0 ? half : N1 - rp;
   const int nbins = rp == 0 ? N2 + 1 : N2;
-  for (uint32_t fr = 0; fr < p.c.nacc; ++fr) {
-    const uint32_t fl = k * p.c.nacc + fr - p.frame0;
-#pragma unroll
-    for (int r = 0; r < 2; ++r) {
-#pragma unroll
-      for (int sq = 0; sq < SEQ; ++sq) {
-        const float4* src = reinterpret_cast<const float4*>(
-            p.scratch + ((static_cast<size_t>(fl) * SEQ + sq) * N1 + (r ? rowB : rowA)) * N2);
-        float2* d = S + (r * SEQ + sq) * Cfg::STRIDE;
-        for (int i = tid; i < N2 / 2; i += Cfg::THREADS) {
-          const float4 q = src[i];
-          d[spad(2 * i)] = make_float2(q.x, q.y);
-          d[spad(2 * i + 1)] = make_float2(q.z, q.w);
-        }
+  const int tid = threadIdx.x;
+  const int slot = tid / Cfg::SLOT_THREADS;
+  const int lt = tid - slot * Cfg::SLOT_THREADS;
+  float2* Z = S + 2 * slot * Cfg::STRIDE;
+  float* A = acc + slot * VA;
+
+  for (int i = tid; i < Cfg::NSLOT * VA; i += Cfg::THREADS) acc[i] = 0.f;
+
+  const uint32_t njobs = p.njobs[k];
+  for (uint32_t it = 0; it < njobs; it += Cfg::NSLOT) {
+    const uint32_t j = it + slot;
+    const bool active = j < njobs;
+    const uint32_t job = active ? p.jobs[k * p.maxjobs + j] : 0u;
+    const uint32_t ga = job_ga(job), gb = job_gb(job);
+    const bool has_b = job_fb(job) != kNoFrame;
+    if (active) {
+      const float2* seq = p.scratch + (static_cast<size_t>(kk) * p.maxjobs + j) * N;
+      for (int i = lt; i < N2; i += Cfg::SLOT_THREADS) {
+        const int r = i / (N2 / 2);
+        const int e = i - r * (N2 / 2);
+        const float4 q = reinterpret_cast<const float4*>(seq + static_cast<size_t>(r ? rowB : rowA) * N2)[e];
+        float2* d = Z + r * Cfg::STRIDE;
+        d[spad(2 * e)] = make_float2(q.x, q.y);
+        d[spad(2 * e + 1)] = make_float2(q.z, q.w);
       }
     }
     __syncthreads();
     {
-      const int sq = tid / Cfg::T2;
-      const int t = tid - sq * Cfg::T2;
-      fft_smem<N2, 16>(S + sq * Cfg::STRIDE, p.tw2, t, true);
+      const int r = lt / Cfg::T2;
+      const int t = lt - r * Cfg::T2;
+      fft_smem<N2, 16>(Z + r * Cfg::STRIDE, p.tw2, t, active);
     }
-    for (int a = tid; a < nbins; a += Cfg::THREADS) {
-      int r, k2, pr, k2p;
-      if (rp != 0) {
-        if (a < N2 / 2) { r = 0; k2 = a; pr = 1; k2p = N2 - 1 - a; }
-        else { r = 1; k2 = a - N2 / 2; pr = 0; k2p = N2 - 1 - k2; }
-      } else {
-        if (a <= N2 / 2) { r = 0; k2 = a; pr = 0; k2p = (N2 - a) & (N2 - 1); }
-        else { r = 1; k2 = a - N2 / 2 - 1; pr = 1; k2p = N2 - 1 - k2; }
-      }
-#pragma unroll
-      for (int sq = 0; sq < SEQ; ++sq) {
-        const float2 za = S[(r * SEQ + sq) * Cfg::STRIDE + spad(k2)];
-        const float2 zb = S[(pr * SEQ + sq) * Cfg::STRIDE + spad(k2p)];
+    if (active) {
+      for (int a = lt; a < nbins; a += Cfg::SLOT_THREADS) {
+        int r, k2, pr, k2p;
+        pair_slot<N2>(rp, a, r, k2, pr, k2p);
+        const float2 za = Z[r * Cfg::STRIDE + spad(k2)];
+        const float2 zb = Z[pr * Cfg::STRIDE + spad(k2p)];
         if constexpr (!DUAL) {
           const float sx = za.x + zb.x, sy = za.y - zb.y;
           const float dx = za.x - zb.x, dy = za.y + zb.y;
-          acc[a] += 0.25f * fmaf(sx, sx, sy * sy);
-          acc[NA + a] += 0.25f * fmaf(dx, dx, dy * dy);
+          A[ga * NA + a] += 0.25f * fmaf(sx, sx, sy * sy);
+          if (has_b) A[gb * NA + a] += 0.25f * fmaf(dx, dx, dy * dy);
         } else {
           const float p1x = 0.5f * (za.x + zb.x), p1y = 0.5f * (za.y - zb.y);
           const float p2x = 0.5f * (za.y + zb.y), p2y = -0.5f * (za.x - zb.x);
           const float a1 = fmaf(p1x, p1x, p1y * p1y);
           const float a2 = fmaf(p2x, p2x, p2y * p2y);
-          acc[(0 + sq) * NA + a] += a1 + a2;
-          acc[(2 + sq) * NA + a] += a1 - a2;
-          acc[(4 + sq) * NA + a] += 2.f * fmaf(p1x, p2x, p1y * p2y);
-          acc[(6 + sq) * NA + a] += -2.f * fmaf(p1y, p2x, -p1x * p2y);
+          A[(0 + ga) * NA + a] += a1 + a2;
+          A[(2 + ga) * NA + a] += a1 - a2;
+          A[(4 + ga) * NA + a] += 2.f * fmaf(p1x, p2x, p1y * p2y);
+          A[(6 + ga) * NA + a] += -2.f * fmaf(p1y, p2x, -p1x * p2y);
         }
       }
     }
     __syncthreads();
   }
+  // gates without data: constant baseline in bin 0 (row pair 0, slot a = 0)
+  if (rp == 0 && tid == 0) {
+    const float n = static_cast<float>(N);
+    for (int gate = 0; gate < 2; ++gate) {
+      const float cnt = static_cast<float>(p.dc[2 * k + gate]);
+      if (cnt == 0.f) continue;
+      if constexpr (!DUAL) {
+        const float d = n * p.c.baselines[gate];
+        acc[gate * NA] += cnt * d * d;
+      } else {
+        const float x = n * p.c.baselines[gate], y = n * p.c.baselines[2 + gate];
+        acc[(0 + gate) * NA] += cnt * (x * x + y * y);
+        acc[(2 + gate) * NA] += cnt * (x * x - y * y);
+        acc[(4 + gate) * NA] += cnt * (2.f * x * y);
+      }
+    }
+  }
+  __syncthreads();
   float* outf = reinterpret_cast<float*>(p.c.out + k * p.c.out_rec);
-  for (int i = tid; i < Cfg::VALS * nbins; i += Cfg::THREADS) {
-    const int v = i / nbins;
-    const int a = i - v * nbins;
+  for (int i = tid; i < VA; i += Cfg::THREADS) {
+    const int v = i / NA;
+    const int a = i - v * NA;
+    if (a >= nbins) continue;
+    float sum = 0.f;
+#pragma unroll
+    for (int sl = 0; sl < Cfg::NSLOT; ++sl) sum += acc[sl * VA + i];
     uint32_t c;
     if (rp != 0) {
       c = a < N2 / 2 ? rp + N1 * a : (N1 - rp) + N1 * (a - N2 / 2);
     } else {
       c = a <= N2 / 2 ? N1 * a : half + N1 * (a - N2 / 2 - 1);
     }
-    outf[static_cast<size_t>(v) * C + c] += acc[v * NA + a];
+    outf[static_cast<size_t>(v) * C + c] += sum;
   }
 }
 
@@ -287,7 +343,7 @@ bool fourstep_supported(int N) {
 template <int N1, bool DUAL>
 static cudaError_t launch_a_n1(int nbits, const FourStepParams& p, cudaStream_t s) {
   using Cfg = PassACfg<N1>;
-  const unsigned grid = p.nframes * (p.N2 / Cfg::BC) * (DUAL ? 2 : 1);
+  const unsigned grid = p.nk * p.maxjobs * (p.N2 / Cfg::BC);
   auto run = [&](auto kern) -> cudaError_t {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(Cfg::SMEM));
@@ -336,8 +392,13 @@ static cudaError_t launch_fs(int nbits, const FourStepParams& p, int pass, cudaS
   return cudaErrorInvalidValue;
 }
 
+// pass: -1 plan, 0 pass A, 1 pass B
 cudaError_t launch_fourstep(int N, int nbits, bool dual, const FourStepParams& p, int pass, cudaStream_t s) {
   (void)N;
+  if (pass < 0) {
+    fourstep_plan_kernel<<<(p.nk + 63) / 64, 64, 0, s>>>(p, dual ? 1 : 0);
+    return cudaGetLastError();
+  }
   return dual ? launch_fs<true>(nbits, p, pass, s) : launch_fs<false>(nbits, p, pass, s);
 }
 

@@ -9,8 +9,11 @@
 //
 // Two real sequences a, b share one complex FFT of z = a + i b:
 //   A(k) = (Z(k) + conj Z(N-k)) / 2 ,  B(k) = (Z(k) - conj Z(N-k)) / (2i).
-// Single pol pairs the two gates of one frame; dual pol pairs the two pols of
-// one gate.
+// Which sequences are paired is decided per frame from the side-channel
+// gates (build_jobs): only gates holding data are transformed; a gate
+// without data is the constant baseline and adds to bin 0 only.
+#include <algorithm>
+
 #include "gspec_kernels.cuh"
 
 namespace gspec {
@@ -93,26 +96,26 @@ __device__ __forceinline__ void commit_stats(const ChainParams& p, const GateSta
 template <int N, bool DUAL>
 struct SmallCfg {
   static constexpr int P = 16;
-  static constexpr int SEQ = DUAL ? 2 : 1;
-  static constexpr int T = N / P;
-  static constexpr int SLOT_THREADS = SEQ * T;
-  static constexpr int NSLOT = SLOT_THREADS >= 256 ? 1 : 256 / SLOT_THREADS;
-  static constexpr int THREADS = NSLOT * SLOT_THREADS;
+  static constexpr int T = N / P;                 // threads per FFT
+  static constexpr int NSLOT = T >= 256 ? 1 : 256 / T;
+  static constexpr int THREADS = NSLOT * T;
   static constexpr int C = N / 2 + 1;
   static constexpr int VALS = DUAL ? 8 : 2;
   static constexpr int SEQ_F2 = spad_size(N);
-  static constexpr size_t SEQ_BYTES = static_cast<size_t>(NSLOT) * SEQ * SEQ_F2 * sizeof(float2);
+  static constexpr int MAX_JOBS = 2 * kMaxUnitFrames;
+  static constexpr size_t SEQ_BYTES = static_cast<size_t>(NSLOT) * SEQ_F2 * sizeof(float2);
   static constexpr size_t ACC_BYTES = static_cast<size_t>(NSLOT) * VALS * C * sizeof(float);
   static constexpr size_t RED_BYTES = static_cast<size_t>(THREADS / 32) * 12 * sizeof(unsigned long long);
-  static constexpr size_t SMEM = SEQ_BYTES + ACC_BYTES + RED_BYTES;
+  static constexpr size_t JOB_BYTES = (MAX_JOBS + 4) * sizeof(uint32_t);
+  static constexpr size_t SMEM = SEQ_BYTES + ACC_BYTES + RED_BYTES + JOB_BYTES;
 };
 
-// One CTA per work unit (output spectrum k, slice); the slice's frames are
-// processed NSLOT at a time, each slot accumulating its frames' spectra in
-// shared memory; slots are summed in a fixed order at the end, so results do
-// not depend on scheduling.
+// One CTA per work unit (output spectrum k, slice of its frames).  The
+// unit's job list (build_jobs) is worked through NSLOT jobs at a time; each
+// slot accumulates its jobs' spectra in shared memory; slots are summed in
+// a fixed order at the end, so results do not depend on scheduling.
 template <int N, int NBITS, bool DUAL>
-__global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS)
+__global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS, 2)
     small_chain_kernel(ChainParams p) {
   using Cfg = SmallCfg<N, DUAL>;
   constexpr int G = Group<NBITS>::samples;
@@ -122,88 +125,111 @@ __global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS)
   static_assert(N % G == 0, "frame must hold whole unpack groups");
 
   extern __shared__ float4 smem_f4[];
-  float2* S = reinterpret_cast<float2*>(smem_f4);
-  float* acc = reinterpret_cast<float*>(reinterpret_cast<char*>(smem_f4) + Cfg::SEQ_BYTES);
-  unsigned long long* red =
-      reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(smem_f4) + Cfg::SEQ_BYTES + Cfg::ACC_BYTES);
+  char* base = reinterpret_cast<char*>(smem_f4);
+  float2* S = reinterpret_cast<float2*>(base);
+  float* acc = reinterpret_cast<float*>(base + Cfg::SEQ_BYTES);
+  unsigned long long* red = reinterpret_cast<unsigned long long*>(base + Cfg::SEQ_BYTES + Cfg::ACC_BYTES);
+  uint32_t* jobs = reinterpret_cast<uint32_t*>(base + Cfg::SEQ_BYTES + Cfg::ACC_BYTES + Cfg::RED_BYTES);
+  uint32_t* jinfo = jobs + Cfg::MAX_JOBS;   // [0] njobs, [1] dc gate 0, [2] dc gate 1
 
   const int tid = threadIdx.x;
-  const int slot = tid / Cfg::SLOT_THREADS;
-  const int lt = tid - slot * Cfg::SLOT_THREADS;
-  const int seq = lt / Cfg::T;
-  const int t = lt - seq * Cfg::T;
+  const int slot = tid / Cfg::T;
+  const int t = tid - slot * Cfg::T;
 
   const uint32_t unit = blockIdx.x;
   const uint32_t k = unit / p.slices;
   const uint32_t sl = unit - k * p.slices;
   const uint32_t f0 = k * p.nacc + sl * p.frames_per_unit;
 
+  if (tid == 0) {
+    uint32_t dc[2];
+    jinfo[0] = build_jobs(p.flags + f0, p.frames_per_unit, DUAL, jobs, dc);
+    jinfo[1] = dc[0];
+    jinfo[2] = dc[1];
+  }
   float bl[2 * NPOL];
 #pragma unroll
   for (int i = 0; i < 2 * NPOL; ++i) bl[i] = p.baselines[i];
-
   for (int i = tid; i < Cfg::NSLOT * Cfg::VALS * C; i += Cfg::THREADS) acc[i] = 0.f;
+  __syncthreads();
+  const uint32_t njobs = jinfo[0];
 
   GateStats st[NPOL];
-  float2* S0 = S + (slot * Cfg::SEQ) * Cfg::SEQ_F2;
-  float2* S1 = S0 + Cfg::SEQ_F2;
+  float2* Z = S + slot * Cfg::SEQ_F2;
   float* A = acc + slot * Cfg::VALS * C;
 
-  for (uint32_t it = 0; it < p.frames_per_unit; it += Cfg::NSLOT) {
-    const uint32_t fl = it + slot;
-    const bool active = fl < p.frames_per_unit;
+  for (uint32_t it = 0; it < njobs; it += Cfg::NSLOT) {
+    const uint32_t jx = it + slot;
+    const bool active = jx < njobs;
+    const uint32_t job = active ? jobs[jx] : 0u;
+    const uint32_t fa = job_fa(job), ga = job_ga(job), fb = job_fb(job), gb = job_gb(job);
     if (active) {
-      const uint32_t f = f0 + fl;
-      for (int gi = lt; gi < NG; gi += Cfg::SLOT_THREADS) {
-        const uint32_t s = f * N + gi * G;
-        float a0[G], a1[G];
-        gate_group<NBITS>(p.g, 0, s, bl[0], bl[1], a0, a1, st[0]);
+#pragma unroll 1
+      for (int gi = t; gi < NG; gi += Cfg::T) {
+        const uint32_t sa = (f0 + fa) * N + gi * G;
+        float re[G], im[G];
         if constexpr (DUAL) {
-          float c0[G], c1[G];
-          gate_group<NBITS>(p.g, 1, s, bl[2], bl[3], c0, c1, st[NPOL - 1]);
-#pragma unroll
-          for (int e = 0; e < G; ++e) {
-            S0[spad(gi * G + e)] = make_float2(a0[e], c0[e]);
-            S1[spad(gi * G + e)] = make_float2(a1[e], c1[e]);
-          }
+          gate_group1<NBITS>(p.g, 0, sa, bl[ga], ga, re, st[0], true);
+          gate_group1<NBITS>(p.g, 1, sa, bl[2 + ga], ga, im, st[NPOL - 1], true);
+        } else if (fb == fa) {
+          gate_group<NBITS>(p.g, 0, sa, bl[0], bl[1], re, im, st[0], 3u);
         } else {
+          gate_group1<NBITS>(p.g, 0, sa, bl[ga], ga, re, st[0], true);
+          if (fb != kNoFrame) {
+            gate_group1<NBITS>(p.g, 0, (f0 + fb) * N + gi * G, bl[gb], gb, im, st[0], true);
+          } else {
 #pragma unroll
-          for (int e = 0; e < G; ++e) S0[spad(gi * G + e)] = make_float2(a0[e], a1[e]);
+            for (int e = 0; e < G; ++e) im[e] = 0.f;
+          }
         }
+#pragma unroll
+        for (int e = 0; e < G; ++e) Z[spad(gi * G + e)] = make_float2(re[e], im[e]);
       }
     }
     __syncthreads();
-    // FFT of every sequence of the slot (contains the barriers)
-    fft_smem<N, Cfg::P>(S0 + seq * Cfg::SEQ_F2, p.tw, t, active);
+    fft_smem<N, Cfg::P>(Z, p.tw, t, active);
     if (active) {
-      for (int c = lt; c < C; c += Cfg::SLOT_THREADS) {
-        const int cm = (N - c) & (N - 1);
+#pragma unroll 1
+      for (int c = t; c < C; c += Cfg::T) {
+        const float2 a = Z[spad(c)], b = Z[spad((N - c) & (N - 1))];
         if constexpr (!DUAL) {
-          const float2 a = S0[spad(c)], b = S0[spad(cm)];
-          // A = Z(c), B = conj Z(N-c)
+          // A = Z(c), B = conj Z(N-c): |A+B|^2/4 and |A-B|^2/4
           const float sx = a.x + b.x, sy = a.y - b.y;
           const float dx = a.x - b.x, dy = a.y + b.y;
-          A[c] += 0.25f * fmaf(sx, sx, sy * sy);
-          A[C + c] += 0.25f * fmaf(dx, dx, dy * dy);
+          A[ga * C + c] += 0.25f * fmaf(sx, sx, sy * sy);
+          if (fb != kNoFrame) A[gb * C + c] += 0.25f * fmaf(dx, dx, dy * dy);
         } else {
-#pragma unroll
-          for (int gate = 0; gate < 2; ++gate) {
-            const float2* Z = gate ? S1 : S0;
-            const float2 a = Z[spad(c)], b = Z[spad(cm)];
-            const float p1x = 0.5f * (a.x + b.x), p1y = 0.5f * (a.y - b.y);
-            const float p2x = 0.5f * (a.y + b.y), p2y = -0.5f * (a.x - b.x);
-            const float a1 = fmaf(p1x, p1x, p1y * p1y);
-            const float a2 = fmaf(p2x, p2x, p2y * p2y);
-            A[(0 + gate) * C + c] += a1 + a2;
-            A[(2 + gate) * C + c] += a1 - a2;
-            A[(4 + gate) * C + c] += 2.f * fmaf(p1x, p2x, p1y * p2y);
-            A[(6 + gate) * C + c] += -2.f * fmaf(p1y, p2x, -p1x * p2y);
-          }
+          const float p1x = 0.5f * (a.x + b.x), p1y = 0.5f * (a.y - b.y);
+          const float p2x = 0.5f * (a.y + b.y), p2y = -0.5f * (a.x - b.x);
+          const float a1 = fmaf(p1x, p1x, p1y * p1y);
+          const float a2 = fmaf(p2x, p2x, p2y * p2y);
+          A[(0 + ga) * C + c] += a1 + a2;
+          A[(2 + ga) * C + c] += a1 - a2;
+          A[(4 + ga) * C + c] += 2.f * fmaf(p1x, p2x, p1y * p2y);
+          A[(6 + ga) * C + c] += -2.f * fmaf(p1y, p2x, -p1x * p2y);
         }
       }
     }
     __syncthreads();
   }
+  // gates without data in a frame: constant baseline, bin 0 only
+  if (tid == 0) {
+    const float n = static_cast<float>(N);
+    for (int gate = 0; gate < 2; ++gate) {
+      const float cnt = static_cast<float>(jinfo[1 + gate]);
+      if (cnt == 0.f) continue;
+      if constexpr (!DUAL) {
+        const float d = n * bl[gate];
+        acc[gate * C] += cnt * d * d;
+      } else {
+        const float x = n * bl[gate], y = n * bl[2 + gate];
+        acc[(0 + gate) * C] += cnt * (x * x + y * y);
+        acc[(2 + gate) * C] += cnt * (x * x - y * y);
+        acc[(4 + gate) * C] += cnt * (2.f * x * y);
+      }
+    }
+  }
+  __syncthreads();
 
   // slots -> output (fixed order)
   float* outf = reinterpret_cast<float*>(p.out + k * p.out_rec);
@@ -220,23 +246,38 @@ __global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS)
   commit_stats<NPOL>(p, st, k, Cfg::VALS * C, red);
 }
 
-// out[k][i] += sum_s partial[k][s][i]  (fixed order)
-__global__ void reduce_partials_kernel(ChainParams p, int vals_c) {
-  const uint32_t k = blockIdx.y;
-  float* outf = reinterpret_cast<float*>(p.out + k * p.out_rec);
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < vals_c; i += gridDim.x * blockDim.x) {
-    float v = 0.f;
-    const float* src = p.partial + static_cast<size_t>(k) * p.slices * vals_c + i;
-    for (uint32_t s = 0; s < p.slices; ++s) v += src[static_cast<size_t>(s) * vals_c];
-    outf[i] += v;
+// Pre-pass of a block: the gate masks of every side-channel item index of
+// one pol (dual: merged items; bit0 gate 0, bit1 gate 1), and per frame the
+// gates holding at least one sample.  The items a frame touches are
+// item_index(first) .. item_index(last) in steps of nsc (the index is
+// monotonic inside a gating chunk and frames never straddle chunks).
+__global__ void gate_prepass_kernel(GateParams g, uint32_t nitems, uint8_t* masks, uint32_t N, uint32_t nframes,
+                                    uint8_t* flags) {
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nitems; i += stride) {
+    bool m0, m1;
+    item_masks(load_item(g, i), g.bitpos, m0, m1);
+    masks[i] = static_cast<uint8_t>(m0 | (m1 << 1));
+  }
+  if (!flags) return;
+  for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < nframes; f += stride) {
+    const uint32_t i0 = item_index(g, f * N), i1 = item_index(g, f * N + N - 1);
+    uint32_t fl = 0;
+    for (uint32_t i = i0; i <= i1; i += g.nsc) {
+      bool m0, m1;
+      item_masks(load_item(g, i), g.bitpos, m0, m1);
+      fl |= m0 | (m1 << 1);
+    }
+    flags[f] = static_cast<uint8_t>(fl);
   }
 }
 
 // Baselines for the next block (edd/src/GatedSpectrometer.cu:98-118), with
 // exact integer sums, an FP64 division and a zero-count guard; then the
 // Stokes record's counter copies (edd/src/GatedSpectrometer.cu:485-525).
-__global__ void finalize_kernel(ChainParams p, int npol, int C, int dual, int convention, float* baselines_out) {
-  const int lane = threadIdx.x;
+// Run by one warp after every counter of the block is final.
+__device__ void finalize_warp(const ChainParams& p, int npol, int C, int dual, int convention, float* baselines_out) {
+  const int lane = threadIdx.x & 31;
   const int vals = dual ? 8 : 2;
   unsigned long long t0 = 0, t1 = 0;
   for (uint32_t k = lane; k < p.n_out; k += 32) {
@@ -265,9 +306,6 @@ __global__ void finalize_kernel(ChainParams p, int npol, int C, int dual, int co
       baselines_out[2 * pol + 0] = den0 ? static_cast<float>(static_cast<double>(s0) / static_cast<double>(den0)) : 0.f;
       baselines_out[2 * pol + 1] = den1 ? static_cast<float>(static_cast<double>(s1) / static_cast<double>(den1)) : 0.f;
     }
-  }
-  __syncwarp();
-  if (lane == 0) {
     for (int i = 0; i < npol * kPolStats; ++i) p.pol_stats[i] = 0;
   }
   if (dual) {
@@ -280,6 +318,26 @@ __global__ void finalize_kernel(ChainParams p, int npol, int C, int dual, int co
       }
     }
   }
+}
+
+__global__ void finalize_kernel(ChainParams p, int npol, int C, int dual, int convention, float* baselines_out) {
+  finalize_warp(p, npol, C, dual, convention, baselines_out);
+}
+
+// out[k][i] += sum_s partial[k][s][i] (fixed order); the last block of the
+// grid also runs the block finalisation (the counters are final already).
+__global__ void reduce_finalize_kernel(ChainParams p, int vals_c, int npol, int C, int dual, int convention,
+                                       float* baselines_out) {
+  const uint32_t k = blockIdx.y;
+  float* outf = reinterpret_cast<float*>(p.out + k * p.out_rec);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < vals_c; i += gridDim.x * blockDim.x) {
+    float v = 0.f;
+    const float* src = p.partial + static_cast<size_t>(k) * p.slices * vals_c + i;
+    for (uint32_t s = 0; s < p.slices; ++s) v += src[static_cast<size_t>(s) * vals_c];
+    outf[i] += v;
+  }
+  if (blockIdx.x == gridDim.x - 1 && blockIdx.y == gridDim.y - 1 && threadIdx.x < 32)
+    finalize_warp(p, npol, C, dual, convention, baselines_out);
 }
 
 // --------------------------------------------------------------- twiddles
@@ -412,10 +470,20 @@ cudaError_t launch_small_chain(int N, int nbits, bool dual, const ChainParams& p
   return dual ? launch_small_d<true>(N, nbits, p, s) : launch_small_d<false>(N, nbits, p, s);
 }
 
-cudaError_t launch_reduce_partials(int N, bool dual, const ChainParams& p, cudaStream_t s) {
-  const int vals_c = (dual ? 8 : 2) * (N / 2 + 1);
+cudaError_t launch_reduce_finalize(int N, bool dual, const ChainParams& p, int npol, int convention,
+                                   float* baselines_out, cudaStream_t s) {
+  const int C = N / 2 + 1;
+  const int vals_c = (dual ? 8 : 2) * C;
   dim3 grid((vals_c + 255) / 256, p.n_out);
-  reduce_partials_kernel<<<grid, 256, 0, s>>>(p, vals_c);
+  reduce_finalize_kernel<<<grid, 256, 0, s>>>(p, vals_c, npol, C, dual ? 1 : 0, convention, baselines_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prepass(const GateParams& g, uint32_t nitems, uint8_t* masks, uint32_t N, uint32_t nframes,
+                           uint8_t* flags, cudaStream_t s) {
+  const uint32_t work = std::max(nitems, nframes);
+  const unsigned grid = std::min<unsigned>(4 * 152, (work + 255) / 256);
+  gate_prepass_kernel<<<grid ? grid : 1, 256, 0, s>>>(g, nitems, masks, N, nframes, flags);
   return cudaGetLastError();
 }
 

@@ -11,8 +11,11 @@ namespace gspec {
 // Per-pol statistics of the block being processed (reset by finalize):
 // [pol][0] n0, [1] n1, [2] sum0 (two's complement), [3] sum1.
 constexpr int kPolStats = 4;
+// Largest number of frames one work unit of the shared-memory path handles.
+constexpr uint32_t kMaxUnitFrames = 1024;
 
 struct ChainParams {
+  const uint8_t* flags;            // per frame of the block: gates holding data
   GateParams g;
   const float* baselines;          // [npol][2]: G0, G1 baselines used for this block
   unsigned long long* pol_stats;   // [npol][kPolStats]
@@ -36,14 +39,17 @@ struct FourStepParams {
   const float2* twA;               // W_N^(m_hi * 1024) , m_hi < N/1024
   const float2* twB;               // W_N^(m_lo), m_lo < 1024
   uint32_t N1, N2;                 // N = N1 * N2; input sample n = N2*n1 + n2
-  uint32_t frame0;                 // first frame held in scratch
-  uint32_t nframes;                // frames of this launch (pass A)
-  uint32_t k0, nk;                 // output spectra of this launch (pass B)
+  uint32_t k0, nk;                 // output spectra of this launch
+  uint32_t maxjobs;                // job slots per output spectrum
+  uint32_t* jobs;                  // [n_out][maxjobs] job list per output spectrum
+  uint32_t* njobs;                 // [n_out]
+  uint32_t* dc;                    // [n_out][2] frames without data per gate
 };
 
 // Host-side launchers (gspec_kernels.cu).
 cudaError_t launch_small_chain(int N, int nbits, bool dual, const ChainParams& p, cudaStream_t s);
-cudaError_t launch_reduce_partials(int N, bool dual, const ChainParams& p, cudaStream_t s);
+cudaError_t launch_reduce_finalize(int N, bool dual, const ChainParams& p, int npol, int convention,
+                                   float* baselines_out, cudaStream_t s);
 cudaError_t launch_finalize(const ChainParams& p, int npol, int C, int dual, int convention, float* baselines_out,
                             cudaStream_t s);
 cudaError_t launch_twiddles(int N, float2* tw, cudaStream_t s);
@@ -52,6 +58,9 @@ cudaError_t launch_gate_debug(int nbits, const GateParams& g, const float* basel
                               float* out, cudaStream_t s);
 cudaError_t launch_unpack(int nbits, const uint8_t* raw, uint64_t nsamples, float* out, cudaStream_t s);
 cudaError_t launch_fourstep(int N, int nbits, bool dual, const FourStepParams& p, int pass, cudaStream_t s);
+// masks of every item; per-frame gate flags when flags != nullptr
+cudaError_t launch_prepass(const GateParams& g, uint32_t nitems, uint8_t* masks, uint32_t N, uint32_t nframes,
+                           uint8_t* flags, cudaStream_t s);
 
 int small_fft_threads(int N, bool dual);
 size_t small_fft_smem(int N, bool dual);
