@@ -460,7 +460,7 @@ gspec_handle* gspec_create(const gspec_config* cfg, char* err, size_t err_len) {
     if (h->nacc > kMaxJobFrames) return bail("more than 16383 frames per output spectrum in one block");
     h->maxjobs = static_cast<uint32_t>(h->nacc * (h->dual ? 2 : 1));
     // scratch of the chunk of output spectra in flight (kept near L2 size)
-    const uint64_t budget = env_u64("GSPEC_SCRATCH_MB", 256) << 20;
+    const uint64_t budget = env_u64("GSPEC_SCRATCH_MB", 512) << 20;
     const uint64_t per_out = static_cast<uint64_t>(h->maxjobs) * static_cast<uint64_t>(N) * sizeof(float2);
     uint64_t kc = budget / per_out;
     if (kc < 1) kc = 1;
