@@ -149,6 +149,24 @@ int gspec_set_baselines(gspec_handle* h, const float* in4);
  * gspec_process (new in this library; no counterpart in the reference). */
 int gspec_get_saturation(gspec_handle* h, uint64_t* out);
 
+/* Allocation-free variant of gspec_run_block_device (no counterpart in the
+ * reference).  For callers that cannot allocate device memory between blocks
+ * (device memory reserved up front by a ring buffer or an outside pool,
+ * real-time loops that must not pay cudaMalloc's latency): one block in
+ * device memory through the chain, accumulated into the caller's d_out
+ * (output layout without the saturation record), with the caller's
+ * d_baselines (4 floats [pol][G0, G1], read and updated for the next block)
+ * on the caller's stream.  No handle, no cudaMalloc/cudaFree: the working
+ * memory is a library-owned device array of GSPEC_NOALLOC_SCRATCH_BYTES held
+ * by every GPU that loads the library.  Only fft_length <= 4096; larger
+ * working sets are rejected (GSPEC_ERR_UNSUPPORTED) with the reason in err.
+ * cfg->device must be the current device; the first call on a device looks
+ * up the array's device address and should come before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race. */
+#define GSPEC_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+int gspec_process_block_noalloc(const gspec_config* cfg, const void* d_block, float* d_baselines, void* d_out,
+                                void* cuda_stream, char* err, size_t err_len);
+
 /* Test entry points of single stages on device memory. */
 /* Unpacker::unpack<nbits> (edd/src/Unpacker.cu:124-140): contiguous packed
  * big-endian samples -> float. */

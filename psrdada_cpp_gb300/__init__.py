@@ -5,6 +5,6 @@ The compute path is the CUDA library ``libgspec.so`` (C ABI in include/gspec.h);
 """
 from .gated_spectrometer import (  # noqa: F401
     DadaBufferLayout, RawBytes, GatedSpectrometer, NullSink, CollectingSink, SimpleFileWriter,
-    GspecError, load_library, unpack_device, file_input_stream,
+    GspecError, GspecConfig, load_library, unpack_device, process_block_noalloc, file_input_stream,
     SINGLE_POL, DUAL_POL, POWER, FULL_STOKES, INTENDED, REFERENCE, FLAG_SATURATION_RECORD,
 )

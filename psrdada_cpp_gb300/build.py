@@ -14,7 +14,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libgspec.so"
-SOURCES = ["gspec_kernels.cu", "gspec_fourstep.cu", "gspec_engine.cu"]
+SOURCES = ["gspec_kernels.cu", "gspec_fourstep.cu", "gspec_engine.cu", "gspec_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 

@@ -17,65 +17,9 @@
 #include "../../include/gspec.h"
 #include "gspec_kernels.cuh"
 
+#include "gspec_engine_internal.cuh"
+
 using namespace gspec;
-
-constexpr int kKernelKinds = 8;
-
-struct gspec_handle {
-  gspec_config cfg{};
-  // layout (edd/src/DadaBufferLayout.cpp:17-39)
-  uint64_t n_heaps = 0, gap = 0, data_bytes = 0, sc_off = 0, sc_bytes = 0;
-  // derived (edd/detail/GatedSpectrometer.cu:99-153)
-  uint64_t nsamps = 0, items_per_pol = 0, n_blocks = 1, batch = 0, nacc = 0, n_out = 0, C = 0;
-  uint64_t rec = 0, out_bytes = 0, ext_bytes = 0;
-  int npol = 1;
-  bool dual = false;
-  int path = 0;
-  uint32_t N1 = 0, N2 = 0;
-  uint32_t slices = 1, frames_per_unit = 1;
-  uint32_t kchunk = 1;
-  int sm_count = 152;
-  std::string err;
-
-  uint8_t* d_in[2] = {nullptr, nullptr};
-  uint8_t* d_out[2] = {nullptr, nullptr};
-  unsigned long long* d_sat[2] = {nullptr, nullptr};
-  unsigned long long* d_sat_dev = nullptr;
-  char* h_out[2] = {nullptr, nullptr};
-  float* d_baselines = nullptr;
-  unsigned long long* d_pol_stats = nullptr;
-  float2* d_tw = nullptr;
-  float2* d_tw1 = nullptr;
-  float2* d_tw2 = nullptr;
-  float2* d_twA = nullptr;
-  float2* d_twB = nullptr;
-  float* d_partial = nullptr;
-  float2* d_scratch = nullptr;
-  uint8_t* d_masks = nullptr;      // per side-channel item index: gates
-  uint8_t* d_flags = nullptr;      // per frame: gates holding data
-  uint32_t* d_jobs = nullptr;      // four-step job lists [kchunk][maxjobs]
-  uint32_t* d_njobs = nullptr;
-  uint32_t* d_dc = nullptr;
-  uint32_t maxjobs = 0;
-  int32_t heap_shift = -1;
-  cudaStream_t h2d = nullptr, proc = nullptr, d2h = nullptr;
-  cudaEvent_t ev_h2d[2] = {}, ev_in_free[2] = {}, ev_out_ready[2] = {};
-  int ia = 1, oa = 0, ha = 0, handed = -1;
-  bool host_written[2] = {false, false};
-  // launch accounting and optional per-kernel event timing
-  uint64_t launches = 0;
-  uint64_t kind_launches[kKernelKinds] = {};
-  int profiling = 0;
-  struct Pending {
-    int kind;
-    cudaEvent_t a, b;
-  };
-  std::vector<Pending> pending;
-  double kind_ms[kKernelKinds] = {};
-  uint64_t kind_timed[kKernelKinds] = {};
-  uint64_t call_count = 0;
-  uint64_t device_bytes = 0;
-};
 
 namespace {
 
@@ -403,6 +347,41 @@ int do_process(gspec_handle* h, const void* block, size_t used, gspec_output* ou
 
 }  // namespace
 
+namespace gspec_engine {
+
+bool configure_handle(gspec_handle* h) { return configure(h); }
+
+// Work units of the shared-memory path: output spectra are split into
+// slices until there are about 8 units per SM and no unit exceeds
+// kMaxUnitFrames frames.
+bool plan_units(gspec_handle* h) {
+  const uint64_t target = env_u64("GSPEC_UNITS", 8ull * h->sm_count);
+  uint64_t s = env_u64("GSPEC_SLICES", 0);
+  if (s == 0) {
+    s = 1;
+    while (h->n_out * s < target && h->nacc % (2 * s) == 0) s *= 2;
+  }
+  while (h->nacc / s > kMaxUnitFrames && h->nacc % (2 * s) == 0) s *= 2;
+  if (h->nacc % s) {
+    h->err = "GSPEC_SLICES must divide the frames per output spectrum";
+    return false;
+  }
+  if (h->nacc / s > kMaxUnitFrames) {
+    h->err = "more than 1024 frames per work unit";
+    return false;
+  }
+  h->slices = static_cast<uint32_t>(s);
+  h->frames_per_unit = static_cast<uint32_t>(h->nacc / s);
+  return true;
+}
+
+cudaError_t run_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out, unsigned long long* d_sat,
+                      cudaStream_t s) {
+  return launch_chain(h, d_block, d_out, d_sat, s);
+}
+
+}  // namespace gspec_engine
+
 extern "C" {
 
 gspec_handle* gspec_create(const gspec_config* cfg, char* err, size_t err_len) {
@@ -445,17 +424,7 @@ gspec_handle* gspec_create(const gspec_config* cfg, char* err, size_t err_len) {
   const uint64_t vals = h->dual ? 8 : 2;
   // work decomposition of the shared-memory path: slices per output spectrum
   if (h->path == 0) {
-    const uint64_t target = env_u64("GSPEC_UNITS", 8ull * h->sm_count);
-    uint64_t s = env_u64("GSPEC_SLICES", 0);
-    if (s == 0) {
-      s = 1;
-      while (h->n_out * s < target && h->nacc % (2 * s) == 0) s *= 2;
-    }
-    while (h->nacc / s > kMaxUnitFrames && h->nacc % (2 * s) == 0) s *= 2;
-    if (h->nacc % s) return bail("GSPEC_SLICES must divide the frames per output spectrum");
-    if (h->nacc / s > kMaxUnitFrames) return bail("more than 1024 frames per work unit");
-    h->slices = static_cast<uint32_t>(s);
-    h->frames_per_unit = static_cast<uint32_t>(h->nacc / s);
+    if (!gspec_engine::plan_units(h)) return bail("");
   } else {
     if (h->nacc > kMaxJobFrames) return bail("more than 16383 frames per output spectrum in one block");
     h->maxjobs = static_cast<uint32_t>(h->nacc * (h->dual ? 2 : 1));

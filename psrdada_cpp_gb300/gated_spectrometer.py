@@ -95,6 +95,7 @@ def load_library() -> ctypes.CDLL:
     lib.gspec_get_profile.argtypes = [vp, ctypes.POINTER(GspecKernelProfile), ctypes.c_int]
     lib.gspec_reset_profile.argtypes = [vp]
     lib.gspec_gate_device.argtypes = [vp, vp, vp, vp]
+    lib.gspec_process_block_noalloc.argtypes = [ctypes.POINTER(GspecConfig), vp, vp, vp, vp, ctypes.c_char_p, sz]
     _LIB = lib
     return lib
 
@@ -328,6 +329,20 @@ class GatedSpectrometer:
 
     def last_error(self) -> str:
         return self._lib.gspec_last_error(self._h).decode()
+
+
+def process_block_noalloc(config: GspecConfig, d_block: int, d_baselines: int, d_out: int, stream: int = 0) -> None:
+    """gspec_process_block_noalloc: one device-resident block through the
+    chain without any device allocation, for callers whose device memory is
+    all reserved up front (see include/gspec.h).  d_baselines (4 float32) is
+    read and updated; d_out accumulates.  Calls that overlap on the GPU race
+    on the library's shared working array."""
+    err = ctypes.create_string_buffer(256)
+    rc = load_library().gspec_process_block_noalloc(ctypes.byref(config), ctypes.c_void_p(d_block),
+                                                    ctypes.c_void_p(d_baselines), ctypes.c_void_p(d_out),
+                                                    ctypes.c_void_p(stream), err, len(err))
+    if rc != GSPEC_OK:
+        raise GspecError(err.value.decode())
 
 
 def unpack_device(d_raw: int, nbits: int, nsamples: int, d_out: int, stream: int = 0) -> None:
