@@ -190,6 +190,68 @@ __device__ __forceinline__ void fft_smem(float2* S, const float2* __restrict__ t
   }
 }
 
+// The same FFT when the input sits unpadded in `src` (a TMA staging buffer):
+// the first pass (span 1, no twiddles) reads src and writes S (padded); the
+// remaining passes run in S.  The caller makes src valid for all threads
+// before the call (mbarrier wait) and S free of readers.
+template <int N, int P>
+__device__ __forceinline__ void fft_smem_from(const float2* src, float2* S, const float2* __restrict__ tw, int t,
+                                              bool active) {
+  constexpr int R = pass_radix(N, 1);
+  constexpr int T = N / P;
+  constexpr int NB = P / R;
+  if (active) {
+#pragma unroll
+    for (int u = 0; u < NB; ++u) {
+      const int j = t + T * u;
+      float2 v[R];
+#pragma unroll
+      for (int k = 0; k < R; ++k) v[k] = src[j + k * (N / R)];
+      dft<R>(v);
+#pragma unroll
+      for (int k = 0; k < R; ++k) S[spad(j * R + k)] = v[k];
+    }
+  }
+  __syncthreads();
+  fft_smem<N, P, R>(S, tw, t, active);
+}
+
+// ------------------------------------------------------- TMA bulk copies
+// One-dimensional bulk copies global -> shared completing on an mbarrier
+// (sm_90+ cp.async.bulk).  Addresses and sizes must be multiples of 16 B.
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+// Waits for the given phase parity; gives up after `limit` polls and
+// returns false (the caller records an error instead of hanging).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
+  const uint32_t a = smem_addr(bar);
+  for (uint32_t i = 0; i < limit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 // ------------------------------------------------------------------ unpack
 // A group is the smallest whole number of samples that starts on a 64-bit
 // word: 8 samples / 8 bytes (8 bit), 32 / 40 (10 bit), 16 / 24 (12 bit).

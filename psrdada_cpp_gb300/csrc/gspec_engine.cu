@@ -177,6 +177,22 @@ cudaError_t timed(gspec_handle* h, int kind, cudaStream_t s, F&& launch) {
   return e;
 }
 
+// Copies the device error word to its pinned host mirror behind the block's
+// kernels (no copy when the caller supplied no mirror).
+cudaError_t refresh_error_word(gspec_handle* h, cudaStream_t s) {
+  if (!h->h_err || !h->d_err) return cudaSuccess;
+  return cudaMemcpyAsync(h->h_err, h->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+}
+
+// Error status of the kernels that completed so far.
+int device_error(gspec_handle* h) {
+  if (h->h_err && *h->h_err) {
+    h->err = "a bounded device wait gave up (code " + std::to_string(*h->h_err) + ")";
+    return GSPEC_ERR_CUDA;
+  }
+  return GSPEC_OK;
+}
+
 cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out, unsigned long long* d_sat,
                          cudaStream_t s) {
   ChainParams p{};
@@ -193,6 +209,7 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
   p.slices = h->slices;
   p.frames_per_unit = h->frames_per_unit;
   p.flags = h->d_flags;
+  p.dev_err = h->d_err;
   const int N = static_cast<int>(h->cfg.fft_length);
   cudaError_t e;
   // gate masks per item and the gates each frame holds data in
@@ -206,10 +223,12 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
     if (e != cudaSuccess) return e;
     if (h->slices > 1) {
       // partial spectra of the slices, then the baselines of the next block
-      return timed(h, 1, s, [&] {
+      e = timed(h, 1, s, [&] {
         return launch_reduce_finalize(N, h->dual, p, h->npol, static_cast<int>(h->cfg.convention), h->d_baselines,
                                       s);
       });
+      if (e != cudaSuccess) return e;
+      return refresh_error_word(h, s);
     }
   } else {
     FourStepParams f{};
@@ -240,10 +259,12 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
       if (e != cudaSuccess) return e;
     }
   }
-  return timed(h, 4, s, [&] {
+  e = timed(h, 4, s, [&] {
     return launch_finalize(p, h->npol, static_cast<int>(h->C), h->dual ? 1 : 0, static_cast<int>(h->cfg.convention),
                            h->d_baselines, s);
   });
+  if (e != cudaSuccess) return e;
+  return refresh_error_word(h, s);
 }
 
 uint64_t env_u64(const char* name, uint64_t dflt) {
@@ -270,9 +291,10 @@ void release(gspec_handle* h) {
   }
   void* ptrs[] = {h->d_sat_dev, h->d_baselines, h->d_pol_stats, h->d_tw,   h->d_tw1,   h->d_tw2,  h->d_twA,
                   h->d_twB,     h->d_partial,   h->d_scratch,   h->d_masks, h->d_flags, h->d_jobs, h->d_njobs,
-                  h->d_dc};
+                  h->d_dc,      h->d_err};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  if (h->h_err) cudaFreeHost(h->h_err);
   if (h->h2d) cudaStreamDestroy(h->h2d);
   if (h->proc) cudaStreamDestroy(h->proc);
   if (h->d2h) cudaStreamDestroy(h->d2h);
@@ -341,6 +363,7 @@ int do_process(gspec_handle* h, const void* block, size_t used, gspec_output* ou
   }
   // the ring buffer releases the block after the call returns
   if (!cuda_ok(h, cudaStreamSynchronize(h->h2d), "H2D")) return GSPEC_ERR_CUDA;
+  if (device_error(h) != GSPEC_OK) return GSPEC_ERR_CUDA;
   if (!cuda_ok(h, cudaPeekAtLastError(), "CUDA")) return GSPEC_ERR_CUDA;
   return GSPEC_OK;
 }
@@ -456,6 +479,11 @@ gspec_handle* gspec_create(const gspec_config* cfg, char* err, size_t err_len) {
   cudaMemset(h->d_baselines, 0, 4 * sizeof(float));
   cudaMemset(h->d_pol_stats, 0, 2 * kPolStats * sizeof(unsigned long long));
   cudaMemset(h->d_sat_dev, 0, h->ext_bytes);
+  if (!dalloc(h, &h->d_err, sizeof(uint32_t), "error word") ||
+      !cuda_ok(h, cudaMallocHost(reinterpret_cast<void**>(&h->h_err), sizeof(uint32_t)), "pinned error word"))
+    return bail("");
+  *h->h_err = 0;
+  cudaMemset(h->d_err, 0, sizeof(uint32_t));
   if (h->path == 0) {
     if (!dalloc(h, &h->d_tw, tw_size(N) * sizeof(float2), "twiddles")) return bail("");
     if (!cuda_ok(h, launch_twiddles(N, h->d_tw, h->proc), "twiddles")) return bail("");
@@ -531,6 +559,7 @@ int gspec_process_device(gspec_handle* h, const void* d_block, size_t used_bytes
 
 int gspec_run_block_device(gspec_handle* h, const void* d_block, void* d_out, void* cuda_stream) {
   if (!h || !d_block || !d_out) return GSPEC_ERR_ARG;
+  if (device_error(h) != GSPEC_OK) return GSPEC_ERR_CUDA;
   cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
   if (!cuda_ok(h, launch_chain(h, static_cast<const uint8_t*>(d_block), static_cast<uint8_t*>(d_out), h->d_sat_dev, s),
                "chain kernels"))

@@ -50,6 +50,8 @@ struct gspec_handle {
   uint32_t* d_dc = nullptr;
   uint32_t maxjobs = 0;
   int32_t heap_shift = -1;
+  uint32_t* d_err = nullptr;       // set by kernels whose bounded waits gave up
+  uint32_t* h_err = nullptr;       // pinned copy, refreshed after every block
   cudaStream_t h2d = nullptr, proc = nullptr, d2h = nullptr;
   cudaEvent_t ev_h2d[2] = {}, ev_in_free[2] = {}, ev_out_ready[2] = {};
   int ia = 1, oa = 0, ha = 0, handed = -1;

@@ -182,15 +182,17 @@ __global__ void __launch_bounds__(PassACfg<N1>::THREADS) fourstep_a_kernel(FourS
 
 template <int N2, bool DUAL>
 struct PassBCfg {
+  static constexpr int THREADS = 256;
   static constexpr int T2 = N2 / 16;
-  static constexpr int SLOT_THREADS = 2 * T2;        // one row pair: rows rp and N1-rp
-  static constexpr int NSLOT = 256 / SLOT_THREADS;   // jobs in flight per CTA
-  static constexpr int THREADS = NSLOT * SLOT_THREADS;
+  static constexpr int JOB_THREADS = 2 * T2;         // one job: rows rp and N1-rp
+  static constexpr int J = THREADS / JOB_THREADS;    // jobs transformed together
   static constexpr int STRIDE = spad_size(N2);
   static constexpr int VALS = DUAL ? 8 : 2;
-  static constexpr int NA = N2 + 1;                  // accumulated bins per row pair
-  static constexpr size_t SMEM = static_cast<size_t>(2 * NSLOT) * STRIDE * sizeof(float2) +
-                                 static_cast<size_t>(VALS) * NSLOT * NA * sizeof(float);
+  static constexpr int BPT = (N2 + 1 + THREADS - 1) / THREADS;   // output bins per thread
+  static constexpr int STAGE_F2 = J * 2 * N2;        // one TMA stage: J jobs x 2 rows, unpadded
+  static constexpr size_t STAGE_BYTES = static_cast<size_t>(STAGE_F2) * sizeof(float2);
+  static constexpr size_t WORK_BYTES = static_cast<size_t>(2 * J) * STRIDE * sizeof(float2);
+  static constexpr size_t SMEM = 2 * STAGE_BYTES + WORK_BYTES + 2 * sizeof(uint64_t);
 };
 
 // Row pair rp holds rows rp and N1-rp (rp = 0: rows 0 and N1/2).  Accumulator
@@ -210,18 +212,25 @@ __device__ __forceinline__ void pair_slot(uint32_t rp, int a, int& r, int& k2, i
   }
 }
 
-// grid.x = nk * N1/2: unit (output spectrum k, row pair rp).  The unit's
-// jobs are spread over NSLOT slots (job j in slot j % NSLOT); every slot
-// accumulates in its own shared-memory spectrum and the slots are summed in
-// a fixed order at the end.
+// grid.x = nk * N1/2: unit (output spectrum k, row pair rp).  J jobs are
+// transformed together (2*T2 threads each).  Their rows arrive by TMA bulk
+// copies into one of two staging buffers while the previous group is
+// transformed; the first FFT pass reads the staging buffer.  Thread t owns
+// output slots a = t + THREADS*i of the pair and keeps their power / Stokes
+// sums in registers over all jobs of the spectrum, adding the jobs in
+// order, so the result does not depend on scheduling.
 template <int N2, bool DUAL>
 __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, 2) fourstep_b_kernel(FourStepParams p) {
   using Cfg = PassBCfg<N2, DUAL>;
-  constexpr int NA = Cfg::NA;
-  constexpr int VA = Cfg::VALS * NA;
+  constexpr int J = Cfg::J;
+  constexpr int BPT = Cfg::BPT;
+  constexpr int VALS = Cfg::VALS;
+  constexpr uint32_t kRowBytes = N2 * sizeof(float2);
   extern __shared__ float4 smem_f4[];
-  float2* S = reinterpret_cast<float2*>(smem_f4);                    // [slot][row r] sequences
-  float* acc = reinterpret_cast<float*>(S + 2 * Cfg::NSLOT * Cfg::STRIDE);   // [slot][v][a]
+  char* base = reinterpret_cast<char*>(smem_f4);
+  float2* stage = reinterpret_cast<float2*>(base);                         // [2][J][2][N2]
+  float2* work = reinterpret_cast<float2*>(base + 2 * Cfg::STAGE_BYTES);   // [J][2][STRIDE]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + 2 * Cfg::STAGE_BYTES + Cfg::WORK_BYTES);
 
   const uint32_t N1 = p.N1;
   const uint32_t N = N1 * N2;
@@ -233,57 +242,99 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, 2) fourstep_b_ker
   const uint32_t rowA = rp, rowB = rp == 0 ? half : N1 - rp;
   const int nbins = rp == 0 ? N2 + 1 : N2;
   const int tid = threadIdx.x;
-  const int slot = tid / Cfg::SLOT_THREADS;
-  const int lt = tid - slot * Cfg::SLOT_THREADS;
-  float2* Z = S + 2 * slot * Cfg::STRIDE;
-  float* A = acc + slot * VA;
-
-  for (int i = tid; i < Cfg::NSLOT * VA; i += Cfg::THREADS) acc[i] = 0.f;
+  const int q = tid / Cfg::JOB_THREADS;            // job of this thread during the FFT
+  const int lt = tid - q * Cfg::JOB_THREADS;
 
   const uint32_t njobs = p.njobs[k];
-  for (uint32_t it = 0; it < njobs; it += Cfg::NSLOT) {
-    const uint32_t j = it + slot;
-    const bool active = j < njobs;
-    const uint32_t job = active ? p.jobs[k * p.maxjobs + j] : 0u;
-    const uint32_t ga = job_ga(job), gb = job_gb(job);
-    const bool has_b = job_fb(job) != kNoFrame;
-    if (active) {
-      const float2* seq = p.scratch + (static_cast<size_t>(kk) * p.maxjobs + j) * N;
-      for (int i = lt; i < N2; i += Cfg::SLOT_THREADS) {
-        const int r = i / (N2 / 2);
-        const int e = i - r * (N2 / 2);
-        const float4 q = reinterpret_cast<const float4*>(seq + static_cast<size_t>(r ? rowB : rowA) * N2)[e];
-        float2* d = Z + r * Cfg::STRIDE;
-        d[spad(2 * e)] = make_float2(q.x, q.y);
-        d[spad(2 * e + 1)] = make_float2(q.z, q.w);
-      }
+  const uint32_t* jobs = p.jobs + k * p.maxjobs;
+  const uint32_t ngroups = (njobs + J - 1) / J;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // thread 0: rows of job group g into stage s
+  auto issue = [&](uint32_t g, int s) {
+    const uint32_t nq = min(static_cast<uint32_t>(J), njobs - g * J);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(&bar[s], nq * 2 * kRowBytes);
+    for (uint32_t qq = 0; qq < nq; ++qq) {
+      const float2* seq = p.scratch + (static_cast<size_t>(kk) * p.maxjobs + g * J + qq) * N;
+      float2* dst = stage + static_cast<size_t>(s) * Cfg::STAGE_F2 + qq * 2 * N2;
+      bulk_g2s(dst, seq + static_cast<size_t>(rowA) * N2, kRowBytes, &bar[s]);
+      bulk_g2s(dst + N2, seq + static_cast<size_t>(rowB) * N2, kRowBytes, &bar[s]);
     }
-    __syncthreads();
+  };
+  if (tid == 0 && ngroups > 0) issue(0, 0);
+
+  float acc[BPT][VALS];
+#pragma unroll
+  for (int i = 0; i < BPT; ++i)
+#pragma unroll
+    for (int v = 0; v < VALS; ++v) acc[i][v] = 0.f;
+
+  for (uint32_t g = 0; g < ngroups; ++g) {
+    const int s = g & 1;
+    if (tid == 0 && g + 1 < ngroups) issue(g + 1, s ^ 1);
+    const bool ok = mbar_wait(&bar[s], (g >> 1) & 1u, 1u << 24);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        if (p.c.dev_err) atomicExch(p.c.dev_err, 2u);
+        // give the copies still in flight a bounded chance to land before exit
+        mbar_wait(&bar[s], (g >> 1) & 1u, 1u << 20);
+        if (g + 1 < ngroups) mbar_wait(&bar[s ^ 1], ((g + 1) >> 1) & 1u, 1u << 20);
+      }
+      __syncthreads();
+      break;
+    }
+    const uint32_t j0 = g * J;
+    const int nq = static_cast<int>(min(static_cast<uint32_t>(J), njobs - j0));
+    const bool active = q < nq;
     {
       const int r = lt / Cfg::T2;
       const int t = lt - r * Cfg::T2;
-      fft_smem<N2, 16>(Z + r * Cfg::STRIDE, p.tw2, t, active);
+      fft_smem_from<N2, 16>(stage + static_cast<size_t>(s) * Cfg::STAGE_F2 + (q * 2 + r) * N2,
+                            work + (2 * q + r) * Cfg::STRIDE, p.tw2, t, active);
     }
-    if (active) {
-      for (int a = lt; a < nbins; a += Cfg::SLOT_THREADS) {
-        int r, k2, pr, k2p;
-        pair_slot<N2>(rp, a, r, k2, pr, k2p);
-        const float2 za = Z[r * Cfg::STRIDE + spad(k2)];
-        const float2 zb = Z[pr * Cfg::STRIDE + spad(k2p)];
+#pragma unroll
+    for (int i = 0; i < BPT; ++i) {
+      const int a = tid + i * Cfg::THREADS;
+      if (a >= nbins) continue;
+      int r, k2, pr, k2p;
+      pair_slot<N2>(rp, a, r, k2, pr, k2p);
+      for (int qq = 0; qq < nq; ++qq) {
+        const uint32_t job = jobs[j0 + qq];
+        const float2 za = work[(2 * qq + r) * Cfg::STRIDE + spad(k2)];
+        const float2 zb = work[(2 * qq + pr) * Cfg::STRIDE + spad(k2p)];
+        const uint32_t ga = job_ga(job);
         if constexpr (!DUAL) {
           const float sx = za.x + zb.x, sy = za.y - zb.y;
           const float dx = za.x - zb.x, dy = za.y + zb.y;
-          A[ga * NA + a] += 0.25f * fmaf(sx, sx, sy * sy);
-          if (has_b) A[gb * NA + a] += 0.25f * fmaf(dx, dx, dy * dy);
+          const float pa = 0.25f * fmaf(sx, sx, sy * sy);
+          const float pb = job_fb(job) != kNoFrame ? 0.25f * fmaf(dx, dx, dy * dy) : 0.f;
+          const uint32_t gb = job_gb(job);
+          acc[i][0] += (ga == 0 ? pa : 0.f) + (gb == 0 ? pb : 0.f);
+          acc[i][1] += (ga == 1 ? pa : 0.f) + (gb == 1 ? pb : 0.f);
         } else {
           const float p1x = 0.5f * (za.x + zb.x), p1y = 0.5f * (za.y - zb.y);
           const float p2x = 0.5f * (za.y + zb.y), p2y = -0.5f * (za.x - zb.x);
           const float a1 = fmaf(p1x, p1x, p1y * p1y);
           const float a2 = fmaf(p2x, p2x, p2y * p2y);
-          A[(0 + ga) * NA + a] += a1 + a2;
-          A[(2 + ga) * NA + a] += a1 - a2;
-          A[(4 + ga) * NA + a] += 2.f * fmaf(p1x, p2x, p1y * p2y);
-          A[(6 + ga) * NA + a] += -2.f * fmaf(p1y, p2x, -p1x * p2y);
+          const float I = a1 + a2, Q = a1 - a2;
+          const float U = 2.f * fmaf(p1x, p2x, p1y * p2y);
+          const float V = -2.f * fmaf(p1y, p2x, -p1x * p2y);
+          if (ga == 0) {
+            acc[i][0] += I;
+            acc[i][2] += Q;
+            acc[i][4] += U;
+            acc[i][6] += V;
+          } else {
+            acc[i][1] += I;
+            acc[i][3] += Q;
+            acc[i][5] += U;
+            acc[i][7] += V;
+          }
         }
       }
     }
@@ -297,31 +348,28 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, 2) fourstep_b_ker
       if (cnt == 0.f) continue;
       if constexpr (!DUAL) {
         const float d = n * p.c.baselines[gate];
-        acc[gate * NA] += cnt * d * d;
+        acc[0][gate] += cnt * d * d;
       } else {
         const float x = n * p.c.baselines[gate], y = n * p.c.baselines[2 + gate];
-        acc[(0 + gate) * NA] += cnt * (x * x + y * y);
-        acc[(2 + gate) * NA] += cnt * (x * x - y * y);
-        acc[(4 + gate) * NA] += cnt * (2.f * x * y);
+        acc[0][0 + gate] += cnt * (x * x + y * y);
+        acc[0][2 + gate] += cnt * (x * x - y * y);
+        acc[0][4 + gate] += cnt * (2.f * x * y);
       }
     }
   }
-  __syncthreads();
   float* outf = reinterpret_cast<float*>(p.c.out + k * p.c.out_rec);
-  for (int i = tid; i < VA; i += Cfg::THREADS) {
-    const int v = i / NA;
-    const int a = i - v * NA;
-    if (a >= nbins) continue;
-    float sum = 0.f;
 #pragma unroll
-    for (int sl = 0; sl < Cfg::NSLOT; ++sl) sum += acc[sl * VA + i];
+  for (int i = 0; i < BPT; ++i) {
+    const int a = tid + i * Cfg::THREADS;
+    if (a >= nbins) continue;
     uint32_t c;
     if (rp != 0) {
       c = a < N2 / 2 ? rp + N1 * a : (N1 - rp) + N1 * (a - N2 / 2);
     } else {
       c = a <= N2 / 2 ? N1 * a : half + N1 * (a - N2 / 2 - 1);
     }
-    outf[static_cast<size_t>(v) * C + c] += sum;
+#pragma unroll
+    for (int v = 0; v < VALS; ++v) outf[static_cast<size_t>(v) * C + c] += acc[i][v];
   }
 }
 

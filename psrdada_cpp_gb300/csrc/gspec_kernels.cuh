@@ -28,6 +28,7 @@ struct ChainParams {
   uint32_t nacc;                   // frames per output spectrum per block
   uint32_t slices;                 // work units per output spectrum
   uint32_t frames_per_unit;
+  uint32_t* dev_err;               // set non-zero when a bounded device wait gives up
 };
 
 // Large-N (four-step) parameters.
