@@ -12,8 +12,10 @@ from pathlib import Path
 
 PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
-BUILD = PKG / "_build"
-LIB = PKG / "libgspec.so"
+BUILD = PKG / os.environ.get("GSPEC_BUILD_DIR", "_build")
+LIB = Path(os.environ["GSPEC_LIB"]) if os.environ.get("GSPEC_LIB") else PKG / "libgspec.so"
+# extra nvcc flags (e.g. -D tuning knobs) and a separate object folder for variant builds
+EXTRA = os.environ.get("GSPEC_NVCC_FLAGS", "").split()
 SOURCES = ["gspec_kernels.cu", "gspec_fourstep.cu", "gspec_engine.cu", "gspec_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
@@ -21,7 +23,7 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 
 def nvcc_flags(extra=()):
     return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-                   "-I", str(PKG.parent / "include")] + list(extra)
+                   "-I", str(PKG.parent / "include")] + EXTRA + list(extra)
 
 
 def _stale(target: Path, deps) -> bool:

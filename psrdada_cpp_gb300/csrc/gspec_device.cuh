@@ -151,9 +151,10 @@ __host__ __device__ constexpr int tw_size(int n) { return tw_offset(n, n); }
 // T = N/P threads with index t of the calling group.  Every thread of the
 // block must call it the same number of times (it contains __syncthreads).
 // tw: per-pass tables, entry [k][q] = exp(-2 pi i q k / (ns R)) at
-// tw_offset(N, ns) + k*ns + q.
+// tw_offset(N, ns) + k*ns + q; the kernels keep a copy in shared memory
+// (load_twiddles) so the passes do not wait on global loads.
 template <int N, int P, int NS = 1>
-__device__ __forceinline__ void fft_smem(float2* S, const float2* __restrict__ tw, int t, bool active) {
+__device__ __forceinline__ void fft_smem(float2* S, const float2* tw, int t, bool active) {
   if constexpr (NS < N) {
     constexpr int R = pass_radix(N, NS);
     constexpr int T = N / P;
@@ -177,7 +178,7 @@ __device__ __forceinline__ void fft_smem(float2* S, const float2* __restrict__ t
         if constexpr (NS > 1) {
           constexpr int TO = tw_offset(N, NS);
 #pragma unroll
-          for (int k = 1; k < R; ++k) v[u][k] = cmul(v[u][k], __ldg(&tw[TO + k * NS + q]));
+          for (int k = 1; k < R; ++k) v[u][k] = cmul(v[u][k], tw[TO + k * NS + q]);
         }
         dft<R>(v[u]);
         const int base = (j - q) * R + q;
@@ -195,8 +196,7 @@ __device__ __forceinline__ void fft_smem(float2* S, const float2* __restrict__ t
 // remaining passes run in S.  The caller makes src valid for all threads
 // before the call (mbarrier wait) and S free of readers.
 template <int N, int P>
-__device__ __forceinline__ void fft_smem_from(const float2* src, float2* S, const float2* __restrict__ tw, int t,
-                                              bool active) {
+__device__ __forceinline__ void fft_smem_from(const float2* src, float2* S, const float2* tw, int t, bool active) {
   constexpr int R = pass_radix(N, 1);
   constexpr int T = N / P;
   constexpr int NB = P / R;
@@ -214,6 +214,14 @@ __device__ __forceinline__ void fft_smem_from(const float2* src, float2* S, cons
   }
   __syncthreads();
   fft_smem<N, P, R>(S, tw, t, active);
+}
+
+// Copies the Stockham tables of an N-point FFT (tw_size(N) entries) from
+// global to shared memory; the caller synchronises before use.
+template <int N>
+__device__ __forceinline__ void load_twiddles(float2* dst, const float2* __restrict__ src) {
+  constexpr int n = tw_size(N);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = __ldg(src + i);
 }
 
 // ------------------------------------------------------- TMA bulk copies
@@ -329,10 +337,12 @@ __device__ __forceinline__ uint32_t item_index(const GateParams& g, uint32_t s) 
 }
 
 // Byte address of pol-stream byte b (dual-pol heaps alternate P0 P1).
+// (pol byte offsets are below 2^32, checked by the host, so 32-bit division)
 __device__ __forceinline__ const uint8_t* pol_byte(const GateParams& g, int pol, uint64_t b) {
   if (!g.dual) return g.block + b;
-  const uint64_t h = b / g.heap_size;
-  return g.block + (2 * h + pol) * g.heap_size + (b - h * g.heap_size);
+  const uint32_t b32 = static_cast<uint32_t>(b);
+  const uint32_t h = b32 / g.heap_size;
+  return g.block + (2ull * h + pol) * g.heap_size + (b32 - h * g.heap_size);
 }
 
 // Selected item after the dual-pol merge (edd/src/GatedSpectrometer.cu:9-19:

@@ -93,6 +93,7 @@ bool configure(gspec_handle* h) {
   if ((pol_bytes * 8) % c.nbits) return fail("pol data is not a whole number of samples");
   h->nsamps = pol_bytes * 8 / c.nbits;
   if (h->nsamps >= (1ull << 32)) return fail("more than 2^32 samples per pol");
+  if (pol_bytes >= (1ull << 32)) return fail("more than 4 GiB of samples per pol in one block");
   h->items_per_pol = h->dual ? h->n_heaps * c.n_side_channels / 2 : h->n_heaps * c.n_side_channels;
   const int gb = group_bytes(c.nbits);
   if (h->dual && (c.heap_size % gb)) {
@@ -375,10 +376,10 @@ namespace gspec_engine {
 bool configure_handle(gspec_handle* h) { return configure(h); }
 
 // Work units of the shared-memory path: output spectra are split into
-// slices until there are about 8 units per SM and no unit exceeds
+// slices until there are about 4 units per SM and no unit exceeds
 // kMaxUnitFrames frames.
 bool plan_units(gspec_handle* h) {
-  const uint64_t target = env_u64("GSPEC_UNITS", 8ull * h->sm_count);
+  const uint64_t target = env_u64("GSPEC_UNITS", 4ull * h->sm_count);
   uint64_t s = env_u64("GSPEC_SLICES", 0);
   if (s == 0) {
     s = 1;

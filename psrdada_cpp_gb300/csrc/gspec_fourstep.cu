@@ -93,7 +93,8 @@ struct PassACfg {
   static constexpr int THREADS = BC * T1;
   static constexpr int STRIDE = spad_size(N1) + 1;  // odd: column-wise reads are conflict-free
   static constexpr size_t RED = static_cast<size_t>(THREADS / 32 > 0 ? THREADS / 32 : 1) * 12 * 8;
-  static constexpr size_t SMEM = static_cast<size_t>(BC) * STRIDE * sizeof(float2) + RED;
+  static constexpr size_t TW_BYTES = static_cast<size_t>(tw_size(N1)) * sizeof(float2);
+  static constexpr size_t SMEM = static_cast<size_t>(BC) * STRIDE * sizeof(float2) + RED + TW_BYTES;
 };
 
 // grid.x = nk * maxjobs * (N2 / BC): (output spectrum, job, column tile)
@@ -107,6 +108,7 @@ __global__ void __launch_bounds__(PassACfg<N1>::THREADS) fourstep_a_kernel(FourS
   float2* S = reinterpret_cast<float2*>(smem_f4);
   unsigned long long* red =
       reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(smem_f4) + BC * Cfg::STRIDE * sizeof(float2));
+  float2* tws = reinterpret_cast<float2*>(reinterpret_cast<char*>(red) + Cfg::RED);
 
   const uint32_t N2 = p.N2;
   const uint32_t N = N1 * N2;
@@ -126,6 +128,7 @@ __global__ void __launch_bounds__(PassACfg<N1>::THREADS) fourstep_a_kernel(FourS
   float bl[2 * NPOL];
 #pragma unroll
   for (int i = 0; i < 2 * NPOL; ++i) bl[i] = p.c.baselines[i];
+  load_twiddles<N1>(tws, p.tw1);
 
   // groups covering this tile's columns of one row
   constexpr int GPR = G <= BC ? BC / G : 1;
@@ -165,24 +168,39 @@ __global__ void __launch_bounds__(PassACfg<N1>::THREADS) fourstep_a_kernel(FourS
   {
     const int sq = tid / Cfg::T1;
     const int t = tid - sq * Cfg::T1;
-    fft_smem<N1, 16>(S + sq * Cfg::STRIDE, p.tw1, t, true);
+    fft_smem<N1, 16>(S + sq * Cfg::STRIDE, tws, t, true);
   }
-  // twiddle W_N^(n2*k1) and store Y[k1][n2]
+  // twiddle W_N^(n2*k1) and store Y[k1][n2].  A thread keeps one column
+  // n2 and steps k1 by KS, so W advances by D = W_N^(n2*KS); the exact
+  // table value is reloaded every 4th point (at most 3 chained products).
   float2* dst = p.scratch + (static_cast<size_t>(kk) * p.maxjobs + j) * N;
-  for (int w = tid; w < BC * N1; w += Cfg::THREADS) {
-    const int col = w % BC;
-    const int k1 = w / BC;
-    const float2 v = S[col * Cfg::STRIDE + spad(k1)];
-    const uint32_t m = (c0 + col) * static_cast<uint32_t>(k1);
-    const float2 W = cmul(__ldg(&p.twA[m >> 10]), __ldg(&p.twB[m & 1023]));
-    dst[static_cast<size_t>(k1) * N2 + c0 + col] = cmul(v, W);
+  {
+    static_assert(Cfg::THREADS % BC == 0, "a thread keeps one column");
+    constexpr int KS = Cfg::THREADS / BC;
+    constexpr int PPT = N1 / KS;
+    const int col = tid % BC;
+    const uint32_t n2 = c0 + col;
+    auto exact = [&](uint32_t m) { return cmul(__ldg(&p.twA[m >> 10]), __ldg(&p.twB[m & 1023])); };
+    const float2 D = exact(n2 * KS);
+    float2 W = make_float2(1.f, 0.f);
+#pragma unroll 4
+    for (int i = 0; i < PPT; ++i) {
+      const int k1 = tid / BC + KS * i;
+      W = (i & 3) == 0 ? exact(n2 * static_cast<uint32_t>(k1)) : cmul(W, D);
+      const float2 v = S[col * Cfg::STRIDE + spad(k1)];
+      dst[static_cast<size_t>(k1) * N2 + n2] = cmul(v, W);
+    }
   }
   commit<NPOL>(p.c, st, k, (DUAL ? 8 : 2) * static_cast<int>(N / 2 + 1), red);
 }
 
+#ifndef GSPEC_PASSB_THREADS
+#define GSPEC_PASSB_THREADS 128
+#endif
+
 template <int N2, bool DUAL>
 struct PassBCfg {
-  static constexpr int THREADS = 256;
+  static constexpr int THREADS = GSPEC_PASSB_THREADS >= 2 * (N2 / 16) ? GSPEC_PASSB_THREADS : 2 * (N2 / 16);
   static constexpr int T2 = N2 / 16;
   static constexpr int JOB_THREADS = 2 * T2;         // one job: rows rp and N1-rp
   static constexpr int J = THREADS / JOB_THREADS;    // jobs transformed together
@@ -192,7 +210,9 @@ struct PassBCfg {
   static constexpr int STAGE_F2 = J * 2 * N2;        // one TMA stage: J jobs x 2 rows, unpadded
   static constexpr size_t STAGE_BYTES = static_cast<size_t>(STAGE_F2) * sizeof(float2);
   static constexpr size_t WORK_BYTES = static_cast<size_t>(2 * J) * STRIDE * sizeof(float2);
-  static constexpr size_t SMEM = 2 * STAGE_BYTES + WORK_BYTES + 2 * sizeof(uint64_t);
+  static constexpr size_t TW_BYTES = static_cast<size_t>(tw_size(N2)) * sizeof(float2);
+  static constexpr size_t JW_BYTES = ((J * sizeof(uint32_t)) + 15) / 16 * 16;
+  static constexpr size_t SMEM = 2 * STAGE_BYTES + WORK_BYTES + TW_BYTES + JW_BYTES + 2 * sizeof(uint64_t);
 };
 
 // Row pair rp holds rows rp and N1-rp (rp = 0: rows 0 and N1/2).  Accumulator
@@ -230,7 +250,10 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, 2) fourstep_b_ker
   char* base = reinterpret_cast<char*>(smem_f4);
   float2* stage = reinterpret_cast<float2*>(base);                         // [2][J][2][N2]
   float2* work = reinterpret_cast<float2*>(base + 2 * Cfg::STAGE_BYTES);   // [J][2][STRIDE]
-  uint64_t* bar = reinterpret_cast<uint64_t*>(base + 2 * Cfg::STAGE_BYTES + Cfg::WORK_BYTES);
+  float2* tws = reinterpret_cast<float2*>(base + 2 * Cfg::STAGE_BYTES + Cfg::WORK_BYTES);
+  uint32_t* jw = reinterpret_cast<uint32_t*>(base + 2 * Cfg::STAGE_BYTES + Cfg::WORK_BYTES + Cfg::TW_BYTES);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + 2 * Cfg::STAGE_BYTES + Cfg::WORK_BYTES + Cfg::TW_BYTES +
+                                              Cfg::JW_BYTES);
 
   const uint32_t N1 = p.N1;
   const uint32_t N = N1 * N2;
@@ -253,6 +276,7 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, 2) fourstep_b_ker
     mbar_init(&bar[1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  load_twiddles<N2>(tws, p.tw2);
   __syncthreads();
   // thread 0: rows of job group g into stage s
   auto issue = [&](uint32_t g, int s) {
@@ -291,11 +315,12 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, 2) fourstep_b_ker
     const uint32_t j0 = g * J;
     const int nq = static_cast<int>(min(static_cast<uint32_t>(J), njobs - j0));
     const bool active = q < nq;
+    if (tid < nq) jw[tid] = jobs[j0 + tid];
     {
       const int r = lt / Cfg::T2;
       const int t = lt - r * Cfg::T2;
       fft_smem_from<N2, 16>(stage + static_cast<size_t>(s) * Cfg::STAGE_F2 + (q * 2 + r) * N2,
-                            work + (2 * q + r) * Cfg::STRIDE, p.tw2, t, active);
+                            work + (2 * q + r) * Cfg::STRIDE, tws, t, active);
     }
 #pragma unroll
     for (int i = 0; i < BPT; ++i) {
@@ -304,7 +329,7 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, 2) fourstep_b_ker
       int r, k2, pr, k2p;
       pair_slot<N2>(rp, a, r, k2, pr, k2p);
       for (int qq = 0; qq < nq; ++qq) {
-        const uint32_t job = jobs[j0 + qq];
+        const uint32_t job = jw[qq];
         const float2 za = work[(2 * qq + r) * Cfg::STRIDE + spad(k2)];
         const float2 zb = work[(2 * qq + pr) * Cfg::STRIDE + spad(k2p)];
         const uint32_t ga = job_ga(job);

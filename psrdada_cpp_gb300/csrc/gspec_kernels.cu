@@ -16,6 +16,12 @@
 
 #include "gspec_kernels.cuh"
 
+// Twiddle tables of the shared-memory path: 1 copies them to shared memory,
+// 0 reads them through the read-only cache.
+#ifndef GSPEC_SMALL_TW_SMEM
+#define GSPEC_SMALL_TW_SMEM 0
+#endif
+
 namespace gspec {
 
 // ------------------------------------------------------------------ helpers
@@ -107,7 +113,8 @@ struct SmallCfg {
   static constexpr size_t ACC_BYTES = static_cast<size_t>(NSLOT) * VALS * C * sizeof(float);
   static constexpr size_t RED_BYTES = static_cast<size_t>(THREADS / 32) * 12 * sizeof(unsigned long long);
   static constexpr size_t JOB_BYTES = (MAX_JOBS + 4) * sizeof(uint32_t);
-  static constexpr size_t SMEM = SEQ_BYTES + ACC_BYTES + RED_BYTES + JOB_BYTES;
+  static constexpr size_t TW_BYTES = static_cast<size_t>(tw_size(N)) * sizeof(float2);
+  static constexpr size_t SMEM = SEQ_BYTES + ACC_BYTES + RED_BYTES + JOB_BYTES + TW_BYTES;
 };
 
 // One CTA per work unit (output spectrum k, slice of its frames).  The
@@ -131,6 +138,7 @@ __global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS, 2)
   unsigned long long* red = reinterpret_cast<unsigned long long*>(base + Cfg::SEQ_BYTES + Cfg::ACC_BYTES);
   uint32_t* jobs = reinterpret_cast<uint32_t*>(base + Cfg::SEQ_BYTES + Cfg::ACC_BYTES + Cfg::RED_BYTES);
   uint32_t* jinfo = jobs + Cfg::MAX_JOBS;   // [0] njobs, [1] dc gate 0, [2] dc gate 1
+  float2* tws = reinterpret_cast<float2*>(base + Cfg::SEQ_BYTES + Cfg::ACC_BYTES + Cfg::RED_BYTES + Cfg::JOB_BYTES);
 
   const int tid = threadIdx.x;
   const int slot = tid / Cfg::T;
@@ -151,6 +159,12 @@ __global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS, 2)
 #pragma unroll
   for (int i = 0; i < 2 * NPOL; ++i) bl[i] = p.baselines[i];
   for (int i = tid; i < Cfg::NSLOT * Cfg::VALS * C; i += Cfg::THREADS) acc[i] = 0.f;
+#if GSPEC_SMALL_TW_SMEM
+  load_twiddles<N>(tws, p.tw);
+  const float2* twp = tws;
+#else
+  const float2* twp = p.tw;
+#endif
   __syncthreads();
   const uint32_t njobs = jinfo[0];
 
@@ -187,7 +201,7 @@ __global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS, 2)
       }
     }
     __syncthreads();
-    fft_smem<N, Cfg::P>(Z, p.tw, t, active);
+    fft_smem<N, Cfg::P>(Z, twp, t, active);
     if (active) {
 #pragma unroll 1
       for (int c = t; c < C; c += Cfg::T) {

@@ -20,7 +20,8 @@ from pathlib import Path
 import numpy as np
 
 _PKG = Path(__file__).resolve().parent
-LIB_PATH = _PKG / "libgspec.so"
+# GSPEC_LIB selects another build of the library (tuning variants)
+LIB_PATH = Path(os.environ["GSPEC_LIB"]) if os.environ.get("GSPEC_LIB") else _PKG / "libgspec.so"
 
 GSPEC_OK, GSPEC_STOP = 0, 1
 SINGLE_POL, DUAL_POL = 0, 1
