@@ -46,6 +46,7 @@ sys.path.insert(0, ROOT)
 METRIC = "input Gsamples/s gated Stokes, BF16-TC vs FP32 at ≤1e-4 err; p99 block latency"
 UNIT = "Gsamples/s"
 FALLBACK_HBM_GBS = 6800.0
+L2_FALLBACK = 129 * 2**20                            # GB300 L2 size when the device does not report it
 
 
 # ------------------------------------------------------------------ helpers
@@ -253,7 +254,11 @@ def run_gpu(args):
                              G.NullSink(), **mk)
     info = gs.info()
     host_blocks = [synth.make_block(spec, seed=1 + rank, block_index=i, kind=kind) for i in range(2)]
-    d_blocks = [torch.from_numpy(b).to(dev) for b in host_blocks]
+    # distinct device copies rotate so that one rotation is at least 3x the L2 size: every step
+    # reads its block from HBM, not from the previous step's L2 lines
+    l2_bytes = int(getattr(torch.cuda.get_device_properties(dev), "L2_cache_size", 0)) or L2_FALLBACK
+    nrot = max(2, -(-3 * l2_bytes // spec.buffer_size))
+    d_blocks = [torch.from_numpy(host_blocks[i % 2]).to(dev) for i in range(nrot)]
     d_out = torch.zeros(int(info.output_bytes), dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
@@ -261,7 +266,7 @@ def run_gpu(args):
     def step(i):
         if i % int(info.n_blocks) == 0:
             d_out.zero_()
-        gs.run_block_device(d_blocks[i % 2].data_ptr(), d_out.data_ptr(), sptr)
+        gs.run_block_device(d_blocks[i % nrot].data_ptr(), d_out.data_ptr(), sptr)
 
     for i in range(args.warmup):
         step(i)
@@ -384,7 +389,7 @@ def run_gpu(args):
             "config": {"workload": spec.name, "fft_length": spec.fft_length, "naccumulate": spec.naccumulate,
                        "nbits": spec.nbits, "pols": spec.npol, "samples_per_pol_per_block": spec.samples_per_pol,
                        "block_bytes": spec.buffer_size, "form": "fp32",
-                       "l2": "inputs larger than L2: two distinct blocks of %d B alternate" % spec.buffer_size,
+                       "l2": "inputs larger than L2: %d device blocks of %d B rotate (L2 %d B)" % (nrot, spec.buffer_size, l2_bytes),
                        "parallelism": f"replicas x{ws} (one independent stream per GPU)"},
             "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "roofline": roofline,
             "cpu_baseline": cpu,
