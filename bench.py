@@ -21,8 +21,8 @@ Stokes, fft 2^16, naccumulate 32, 2^26 samples per pol per block.
               on this host's cores, on a bounded sample of the workload.
 
 ``--impl reference`` times that CPU restatement alone (the reference has no
-CPU implementation of its own and its GPU code cannot be built here; see
-the design doc) on the same metric, each step one output spectrum's worth of
+CPU implementation of its own, and its GPU chain needs libpsrdada, Boost and
+cuFFT, none of which is installed) on the same metric, each step one output spectrum's worth of
 input.  Under torchrun every rank runs its own stream on its own GPU
 (replicas, weak scaling); rank 0 prints the line.
 """

@@ -37,12 +37,14 @@ extern "C" {
 #define GSPEC_POWER 0       /* GatedPowerSpectrumOutput */
 #define GSPEC_FULL_STOKES 1 /* GatedFullStokesOutput    */
 
-/* Gate-index convention. */
+/* Gate-index convention of the side-channel items. */
 #define GSPEC_INTENDED 0  /* item of the heap holding the sample; per-pol baselines */
 #define GSPEC_REFERENCE 1 /* the reference's literal indexing where it stays in bounds */
 
 /* Flags. */
 #define GSPEC_FLAG_SATURATION_RECORD 1u /* append n_out x {sat G0, sat G1} u64 to each output */
+#define GSPEC_FLAG_NO_HOST_BUFFERS 2u   /* no pinned output buffers: the handle is driven only through
+                                           gspec_run_block_device, a gspec_server or a gspec_batch */
 
 typedef struct gspec_config {
   /* DadaBufferLayout (edd/DadaBufferLayout.hpp:20-54): the reference reads the
@@ -64,6 +66,11 @@ typedef struct gspec_config {
   float output_level;
   int32_t device;                 /* CUDA device ordinal */
   uint32_t flags;
+  /* Schedule overrides (new in this library; 0 keeps the built-in choice).
+   * The autotuner (psrdada_cpp_gb300.autotune) sets them per stream shape. */
+  uint64_t tune_units;            /* shared-memory path: target work units per block (default 4 x SMs) */
+  uint32_t tune_n1;               /* four-step path: first-pass length N1 (N2 = fft_length/N1 in [128, 1024]) */
+  uint32_t tune_scratch_mb;       /* four-step path: scratch budget of one chunk of spectra (default 512 MiB) */
 } gspec_config;
 
 typedef struct gspec_info {
@@ -130,6 +137,10 @@ int gspec_process_device(gspec_handle* h, const void* d_block, size_t used_bytes
 int gspec_run_block_device(gspec_handle* h, const void* d_block, void* d_out, void* cuda_stream);
 
 int gspec_get_info(const gspec_handle* h, gspec_info* info);
+/* Sizes of a handle for cfg without creating it (no reference counterpart):
+ * fills info (kernel_launches = 0) including device_bytes, the device memory
+ * gspec_create would allocate.  Needs the device to read its SM count. */
+int gspec_query(const gspec_config* cfg, gspec_info* info, char* err, size_t err_len);
 
 /* Kernel accounting (new in this library; no counterpart in the reference):
  * with profiling enabled every kernel launch is bracketed by CUDA events on
@@ -166,6 +177,101 @@ int gspec_get_saturation(gspec_handle* h, uint64_t* out);
 #define GSPEC_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 int gspec_process_block_noalloc(const gspec_config* cfg, const void* d_block, float* d_baselines, void* d_out,
                                 void* cuda_stream, char* err, size_t err_len);
+
+/* ------------------------------------------------------------------------
+ * Serving (no reference counterpart: the reference runs one
+ * GatedSpectrometer per process on one ring buffer).  One server owns one
+ * GPU and a scheduler thread that takes blocks from many concurrent streams
+ * (each with its own fft_length, naccumulate, bit depth and pol mode), keeps
+ * every admitted stream's baselines, counters and output accumulators
+ * resident in device memory, and overlaps the streams' work on the device.
+ * A stream is admitted when the device memory it needs (gspec_query) fits
+ * into the memory budget next to the streams already admitted; until then it
+ * and its blocks wait in FIFO order.  Blocks of one stream are processed in
+ * submission order; each produces one result.  A result carries the output
+ * block (reference layout, plus the saturation record with
+ * GSPEC_FLAG_SATURATION_RECORD) when that block completed one, i.e. every
+ * n_blocks blocks, with no reference pipeline delay.
+ * ------------------------------------------------------------------------ */
+typedef struct gspec_server gspec_server;
+typedef struct gspec_server_config {
+  uint64_t memory_budget;   /* bytes of device memory all admitted streams may hold */
+  int32_t device;
+  int32_t max_inflight;     /* blocks of one stream on the GPU at once (1 or 2; 0 = 2) */
+  int32_t output_buffers;   /* pinned host output buffers per stream (0 = 2) */
+  int32_t reserved;
+} gspec_server_config;
+typedef struct gspec_result {
+  int32_t stream;           /* stream id */
+  int32_t status;           /* GSPEC_OK or a negative error code */
+  uint64_t tag;             /* the caller's tag of the block */
+  uint64_t block_index;     /* 0-based block number within the stream */
+  const char* data;         /* output block, or NULL when the block completed none */
+  uint64_t size;
+  int32_t buffer;           /* pass to gspec_server_release once data has been consumed */
+  int32_t reserved;
+  double t_submit;          /* seconds on the server clock: gspec_submit called */
+  double t_start;           /* the block's first copy was issued to the GPU */
+  double t_done;            /* output on the host (or the block finished) */
+} gspec_result;
+gspec_server* gspec_server_create(const gspec_server_config* cfg, char* err, size_t err_len);
+/* Waits for the streams' outstanding blocks, then frees everything. */
+void gspec_server_destroy(gspec_server* s);
+/* Opens a stream; *stream_id receives its id.  GSPEC_OK when it was
+ * admitted or queued for admission, GSPEC_ERR_ARG when cfg is invalid or it
+ * can never fit into the budget. */
+int gspec_stream_open(gspec_server* s, const gspec_config* cfg, int* stream_id);
+/* 0 waiting for admission, 1 admitted, 2 closing, 3 closed, <0 unknown id. */
+int gspec_stream_state(gspec_server* s, int stream_id);
+/* Queues one block.  The host memory must stay valid and unchanged until
+ * the block's result has been returned by gspec_poll; page-locked memory
+ * lets its copy overlap the GPU work of other blocks. */
+int gspec_submit(gspec_server* s, int stream_id, const void* block, size_t size, uint64_t tag);
+/* Returns up to max finished results (oldest first), waiting up to
+ * timeout_us microseconds for the first one. */
+int gspec_poll(gspec_server* s, gspec_result* results, int max, int timeout_us);
+/* Gives an output buffer back to its stream. */
+int gspec_server_release(gspec_server* s, int stream_id, int buffer);
+/* Closes a stream once its queued blocks are done and frees its memory,
+ * which may admit waiting streams. */
+int gspec_stream_close(gspec_server* s, int stream_id);
+double gspec_server_now(const gspec_server* s);
+uint64_t gspec_server_memory_in_use(const gspec_server* s);
+/* Kernels launched by all streams so far. */
+uint64_t gspec_server_kernel_launches(const gspec_server* s);
+const char* gspec_server_last_error(const gspec_server* s);
+
+/* ------------------------------------------------------------------------
+ * Batch of uneven streams in one CUDA graph (no reference counterpart).
+ * Each member stream has its own configuration and device input block;
+ * gspec_batch_run launches one graph in which every stream's chain runs in
+ * its own branch, so the streams' kernels share the GPU.  Member i's output
+ * accumulator is complete after the steps where (step + 1) % n_blocks_i == 0.
+ * ------------------------------------------------------------------------ */
+typedef struct gspec_batch gspec_batch;
+gspec_batch* gspec_batch_create(const gspec_config* cfgs, int n, char* err, size_t err_len);
+void gspec_batch_destroy(gspec_batch* b);
+int gspec_batch_size(const gspec_batch* b);
+int gspec_batch_get_info(const gspec_batch* b, int i, gspec_info* info);
+/* Device input block of member i (buffer_size bytes), read by the next run. */
+void* gspec_batch_input(gspec_batch* b, int i);
+/* Copies one block (host or device memory, buffer_size bytes) into member
+ * i's input on the caller's stream. */
+int gspec_batch_set_input(gspec_batch* b, int i, const void* src, size_t bytes, void* cuda_stream);
+/* Copies member i's output accumulator (output layout without the
+ * saturation record) to dst (host or device memory) on the caller's stream
+ * and waits for the copy. */
+int gspec_batch_read_output(gspec_batch* b, int i, void* dst, size_t bytes, void* cuda_stream);
+/* Device output accumulator of member i (output layout without the
+ * saturation record) and whether the last run completed it. */
+int gspec_batch_output(gspec_batch* b, int i, void** d_out, uint64_t* bytes, int* complete);
+/* One step: one block through every member, as one graph launch on the
+ * caller's stream (captured at the first call). */
+int gspec_batch_run(gspec_batch* b, void* cuda_stream);
+/* Kernel nodes in one step's graph and steps run so far. */
+uint64_t gspec_batch_kernels_per_step(const gspec_batch* b);
+uint64_t gspec_batch_steps(const gspec_batch* b);
+const char* gspec_batch_last_error(const gspec_batch* b);
 
 /* Test entry points of single stages on device memory. */
 /* Unpacker::unpack<nbits> (edd/src/Unpacker.cu:124-140): contiguous packed

@@ -1,7 +1,7 @@
 /*
  * CPU restatement of the EDD gated-spectrometer chain in C with OpenMP.
  *
- * TEST / BASELINE INFRASTRUCTURE ONLY: used by tests/ as a second checker and
+ * TEST AND CPU-BASELINE INFRASTRUCTURE ONLY: used by tests/ as a second checker and
  * by bench.py as the timed CPU path ("cpu_baseline", "--impl reference").
  * The product path never links it.
  *

@@ -1,5 +1,5 @@
 """ctypes wrapper of oracle/libgspec_cpu.so, the C/OpenMP restatement of the
-chain (TEST / BASELINE INFRASTRUCTURE ONLY: imported by tests/ and by
+chain (TEST AND CPU-BASELINE INFRASTRUCTURE ONLY: imported by tests/ and by
 bench.py's CPU legs)."""
 from __future__ import annotations
 

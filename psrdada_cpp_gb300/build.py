@@ -16,7 +16,8 @@ BUILD = PKG / os.environ.get("GSPEC_BUILD_DIR", "_build")
 LIB = Path(os.environ["GSPEC_LIB"]) if os.environ.get("GSPEC_LIB") else PKG / "libgspec.so"
 # extra nvcc flags (e.g. -D tuning knobs) and a separate object folder for variant builds
 EXTRA = os.environ.get("GSPEC_NVCC_FLAGS", "").split()
-SOURCES = ["gspec_kernels.cu", "gspec_fourstep.cu", "gspec_engine.cu", "gspec_noalloc.cu"]
+SOURCES = ["gspec_kernels.cu", "gspec_fourstep.cu", "gspec_engine.cu", "gspec_noalloc.cu", "gspec_server.cu",
+           "gspec_batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 
@@ -55,7 +56,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_v: bool = False) -> 
     if failed:
         raise RuntimeError(f"nvcc failed for {failed}")
     if force or procs or _stale(LIB, objs):
-        cmd = [NVCC] + ARCH + ["-shared", "-o", str(LIB)] + [str(o) for o in objs] + ["-lcudart"]
+        cmd = [NVCC] + ARCH + ["-shared", "-o", str(LIB)] + [str(o) for o in objs] + ["-lcudart", "-lpthread"]
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.run(cmd, check=True)

@@ -76,6 +76,13 @@ bool configure(gspec_handle* h) {
     h->path = 1;
     h->N1 = fourstep_n1(static_cast<int>(N));
     h->N2 = fourstep_n2(static_cast<int>(N));
+    if (c.tune_n1) {
+      const uint64_t n1 = c.tune_n1;
+      if ((n1 & (n1 - 1)) || n1 < 64 || n1 > 1024 || N % n1 || N / n1 < 128 || N / n1 > 1024)
+        return fail("tune_n1 must be a power of two in [64, 1024] with fft_length/tune_n1 in [128, 1024]");
+      h->N1 = static_cast<uint32_t>(n1);
+      h->N2 = static_cast<uint32_t>(N / n1);
+    }
   } else {
     return fail("fft_length must be in [32, 2^20]");
   }
@@ -317,6 +324,7 @@ int do_process(gspec_handle* h, const void* block, size_t used, gspec_output* ou
                        std::to_string(h->cfg.buffer_size) + " byte");
   }
   if (!block) return set_err(h, GSPEC_ERR_ARG, "null block");
+  if (!h->h_out[0]) return set_err(h, GSPEC_ERR_STATE, "handle was created with GSPEC_FLAG_NO_HOST_BUFFERS");
   // input double buffer: buffer a receives block n (edd/detail/GatedSpectrometer.cu:314-316)
   h->ia ^= 1;
   const int ia = h->ia, ib = ia ^ 1;
@@ -379,7 +387,7 @@ bool configure_handle(gspec_handle* h) { return configure(h); }
 // slices until there are about 4 units per SM and no unit exceeds
 // kMaxUnitFrames frames.
 bool plan_units(gspec_handle* h) {
-  const uint64_t target = env_u64("GSPEC_UNITS", 4ull * h->sm_count);
+  const uint64_t target = h->cfg.tune_units ? h->cfg.tune_units : env_u64("GSPEC_UNITS", 4ull * h->sm_count);
   uint64_t s = env_u64("GSPEC_SLICES", 0);
   if (s == 0) {
     s = 1;
@@ -402,6 +410,68 @@ bool plan_units(gspec_handle* h) {
 cudaError_t run_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out, unsigned long long* d_sat,
                       cudaStream_t s) {
   return launch_chain(h, d_block, d_out, d_sat, s);
+}
+
+// Device-dependent planning after configure_handle: SM count, work units of
+// the shared-memory path, job slots and scratch chunk of the four-step path.
+bool plan_handle(gspec_handle* h) {
+  cudaDeviceProp prop{};
+  if (cudaGetDeviceProperties(&prop, h->cfg.device) != cudaSuccess) {
+    h->err = "cannot read the properties of device " + std::to_string(h->cfg.device);
+    return false;
+  }
+  h->sm_count = prop.multiProcessorCount;
+  if (h->path == 0) return plan_units(h);
+  if (h->nacc > kMaxJobFrames) {
+    h->err = "more than 16383 frames per output spectrum in one block";
+    return false;
+  }
+  h->maxjobs = static_cast<uint32_t>(h->nacc * (h->dual ? 2 : 1));
+  // scratch of the chunk of output spectra in flight
+  const uint64_t mb = h->cfg.tune_scratch_mb ? h->cfg.tune_scratch_mb : env_u64("GSPEC_SCRATCH_MB", 512);
+  const uint64_t per_out = static_cast<uint64_t>(h->maxjobs) * h->cfg.fft_length * sizeof(float2);
+  uint64_t kc = (mb << 20) / per_out;
+  if (kc < 1) kc = 1;
+  if (kc > h->n_out) kc = h->n_out;
+  h->kchunk = static_cast<uint32_t>(kc);
+  return true;
+}
+
+// Device bytes gspec_create allocates for a planned handle (the same list
+// and the same 16-byte minimum as its dalloc calls).
+uint64_t footprint(const gspec_handle* h) {
+  auto sz = [](uint64_t b) { return b ? b : 16; };
+  const uint64_t N = h->cfg.fft_length;
+  const uint64_t vals = h->dual ? 8 : 2;
+  uint64_t t = sz(h->items_per_pol) + sz(h->batch);
+  t += 2 * (sz(h->cfg.buffer_size) + sz(h->out_bytes) + sz(h->ext_bytes));
+  t += sz(h->ext_bytes) + sz(4 * sizeof(float)) + sz(2 * kPolStats * sizeof(unsigned long long)) + sz(sizeof(uint32_t));
+  if (h->path == 0) {
+    t += sz(tw_size(static_cast<int>(N)) * sizeof(float2));
+    if (h->slices > 1) t += sz(h->n_out * h->slices * vals * h->C * sizeof(float));
+  } else {
+    t += sz(tw_size(static_cast<int>(h->N1)) * sizeof(float2)) + sz(tw_size(static_cast<int>(h->N2)) * sizeof(float2));
+    t += 2 * sz(1024 * sizeof(float2));
+    t += sz(static_cast<uint64_t>(h->kchunk) * h->maxjobs * N * sizeof(float2));
+    t += sz(h->n_out * h->maxjobs * sizeof(uint32_t)) + sz(h->n_out * sizeof(uint32_t)) +
+         sz(2ull * h->n_out * sizeof(uint32_t));
+  }
+  return t;
+}
+
+void fill_info(const gspec_handle* h, gspec_info* info) {
+  info->nchans = h->C;
+  info->n_out = h->n_out;
+  info->n_blocks = h->n_blocks;
+  info->nsamps_per_pol = h->nsamps;
+  info->batch = h->batch;
+  info->output_bytes = h->out_bytes + ((h->cfg.flags & GSPEC_FLAG_SATURATION_RECORD) ? h->ext_bytes : 0);
+  info->record_bytes = h->rec;
+  info->device_bytes = h->device_bytes;
+  info->fft_path = static_cast<uint64_t>(h->path);
+  info->n1 = h->N1;
+  info->n2 = h->N2;
+  info->kernel_launches = h->launches;
 }
 
 }  // namespace gspec_engine
@@ -432,8 +502,7 @@ gspec_handle* gspec_create(const gspec_config* cfg, char* err, size_t err_len) {
     return nullptr;
   };
   if (cudaSetDevice(cfg->device) != cudaSuccess) return bail("cudaSetDevice failed");
-  cudaDeviceProp prop{};
-  if (cudaGetDeviceProperties(&prop, cfg->device) == cudaSuccess) h->sm_count = prop.multiProcessorCount;
+  if (!gspec_engine::plan_handle(h)) return bail("");
   if (!cuda_ok(h, cudaStreamCreateWithFlags(&h->h2d, cudaStreamNonBlocking), "stream") ||
       !cuda_ok(h, cudaStreamCreateWithFlags(&h->proc, cudaStreamNonBlocking), "stream") ||
       !cuda_ok(h, cudaStreamCreateWithFlags(&h->d2h, cudaStreamNonBlocking), "stream"))
@@ -446,30 +515,18 @@ gspec_handle* gspec_create(const gspec_config* cfg, char* err, size_t err_len) {
   }
   const int N = static_cast<int>(cfg->fft_length);
   const uint64_t vals = h->dual ? 8 : 2;
-  // work decomposition of the shared-memory path: slices per output spectrum
-  if (h->path == 0) {
-    if (!gspec_engine::plan_units(h)) return bail("");
-  } else {
-    if (h->nacc > kMaxJobFrames) return bail("more than 16383 frames per output spectrum in one block");
-    h->maxjobs = static_cast<uint32_t>(h->nacc * (h->dual ? 2 : 1));
-    // scratch of the chunk of output spectra in flight (kept near L2 size)
-    const uint64_t budget = env_u64("GSPEC_SCRATCH_MB", 512) << 20;
-    const uint64_t per_out = static_cast<uint64_t>(h->maxjobs) * static_cast<uint64_t>(N) * sizeof(float2);
-    uint64_t kc = budget / per_out;
-    if (kc < 1) kc = 1;
-    if (kc > h->n_out) kc = h->n_out;
-    h->kchunk = static_cast<uint32_t>(kc);
-  }
   if (!dalloc(h, &h->d_masks, h->items_per_pol, "gate masks") || !dalloc(h, &h->d_flags, h->batch, "frame flags"))
     return bail("");
   for (int i = 0; i < 2; ++i) {
     if (!dalloc(h, &h->d_in[i], cfg->buffer_size, "input") || !dalloc(h, &h->d_out[i], h->out_bytes, "output") ||
         !dalloc(h, &h->d_sat[i], h->ext_bytes, "saturation"))
       return bail("");
-    if (!cuda_ok(h, cudaMallocHost(reinterpret_cast<void**>(&h->h_out[i]), h->out_bytes + h->ext_bytes),
-                 "pinned output"))
-      return bail("");
-    std::memset(h->h_out[i], 0, h->out_bytes + h->ext_bytes);
+    if (!(cfg->flags & GSPEC_FLAG_NO_HOST_BUFFERS)) {
+      if (!cuda_ok(h, cudaMallocHost(reinterpret_cast<void**>(&h->h_out[i]), h->out_bytes + h->ext_bytes),
+                   "pinned output"))
+        return bail("");
+      std::memset(h->h_out[i], 0, h->out_bytes + h->ext_bytes);
+    }
     if (!cuda_ok(h, cudaMemset(h->d_out[i], 0, h->out_bytes), "memset") ||
         !cuda_ok(h, cudaMemset(h->d_sat[i], 0, h->ext_bytes), "memset"))
       return bail("");
@@ -570,18 +627,30 @@ int gspec_run_block_device(gspec_handle* h, const void* d_block, void* d_out, vo
 
 int gspec_get_info(const gspec_handle* h, gspec_info* info) {
   if (!h || !info) return GSPEC_ERR_ARG;
-  info->nchans = h->C;
-  info->n_out = h->n_out;
-  info->n_blocks = h->n_blocks;
-  info->nsamps_per_pol = h->nsamps;
-  info->batch = h->batch;
-  info->output_bytes = h->out_bytes + ((h->cfg.flags & GSPEC_FLAG_SATURATION_RECORD) ? h->ext_bytes : 0);
-  info->record_bytes = h->rec;
-  info->device_bytes = h->device_bytes;
-  info->fft_path = static_cast<uint64_t>(h->path);
-  info->n1 = h->N1;
-  info->n2 = h->N2;
-  info->kernel_launches = h->launches;
+  gspec_engine::fill_info(h, info);
+  return GSPEC_OK;
+}
+
+int gspec_query(const gspec_config* cfg, gspec_info* info, char* err, size_t err_len) {
+  auto report = [&](const std::string& m) {
+    if (err && err_len) std::snprintf(err, err_len, "%s", m.c_str());
+  };
+  if (!cfg || !info) {
+    report("null argument");
+    return GSPEC_ERR_ARG;
+  }
+  gspec_handle h;
+  h.cfg = *cfg;
+  if (!configure(&h)) {
+    report(h.err);
+    return GSPEC_ERR_ARG;
+  }
+  if (!gspec_engine::plan_handle(&h)) {
+    report(h.err);
+    return GSPEC_ERR_ARG;
+  }
+  h.device_bytes = gspec_engine::footprint(&h);
+  gspec_engine::fill_info(&h, info);
   return GSPEC_OK;
 }
 

@@ -77,6 +77,11 @@ namespace gspec_engine {
 bool configure_handle(gspec_handle* h);
 // Slices per output spectrum of the shared-memory path (needs h->sm_count).
 bool plan_units(gspec_handle* h);
+// SM count, work units / scratch chunk (after configure_handle).
+bool plan_handle(gspec_handle* h);
+// Device bytes gspec_create allocates for a planned handle.
+uint64_t footprint(const gspec_handle* h);
+void fill_info(const gspec_handle* h, gspec_info* info);
 // Enqueues the whole chain for one block on stream s using h's buffers.
 cudaError_t run_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out, unsigned long long* d_sat,
                       cudaStream_t s);

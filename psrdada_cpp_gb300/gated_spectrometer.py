@@ -28,6 +28,8 @@ SINGLE_POL, DUAL_POL = 0, 1
 POWER, FULL_STOKES = 0, 1
 INTENDED, REFERENCE = 0, 1
 FLAG_SATURATION_RECORD = 1
+FLAG_NO_HOST_BUFFERS = 2
+TUNE_KEYS = ("tune_units", "tune_n1", "tune_scratch_mb")
 
 
 class GspecConfig(ctypes.Structure):
@@ -47,6 +49,9 @@ class GspecConfig(ctypes.Structure):
         ("output_level", ctypes.c_float),
         ("device", ctypes.c_int32),
         ("flags", ctypes.c_uint32),
+        ("tune_units", ctypes.c_uint64),
+        ("tune_n1", ctypes.c_uint32),
+        ("tune_scratch_mb", ctypes.c_uint32),
     ]
 
 
@@ -97,6 +102,9 @@ def load_library() -> ctypes.CDLL:
     lib.gspec_reset_profile.argtypes = [vp]
     lib.gspec_gate_device.argtypes = [vp, vp, vp, vp]
     lib.gspec_process_block_noalloc.argtypes = [ctypes.POINTER(GspecConfig), vp, vp, vp, vp, ctypes.c_char_p, sz]
+    lib.gspec_query.argtypes = [ctypes.POINTER(GspecConfig), ctypes.POINTER(GspecInfo), ctypes.c_char_p, sz]
+    from . import serving
+    serving.declare(lib)
     _LIB = lib
     return lib
 
@@ -220,7 +228,7 @@ class GatedSpectrometer:
                  fft_length: int, naccumulate: int, nbits: int, input_level: float,
                  output_level: float, handler, input_type: int = SINGLE_POL,
                  output_type: int | None = None, convention: int = INTENDED, device: int = 0,
-                 flags: int = 0):
+                 flags: int = 0, tune: dict | None = None):
         self._lib = load_library()
         if output_type is None:
             output_type = FULL_STOKES if input_type == DUAL_POL else POWER
@@ -229,7 +237,8 @@ class GatedSpectrometer:
             n_side_channels=layout.getNSideChannels(), selected_side_channel=selectedSideChannel,
             selected_bit=selectedBit, fft_length=fft_length, naccumulate=naccumulate, nbits=nbits,
             input_type=input_type, output_type=output_type, convention=convention,
-            input_level=input_level, output_level=output_level, device=device, flags=flags)
+            input_level=input_level, output_level=output_level, device=device, flags=flags,
+            **{k: int(v) for k, v in (tune or {}).items() if k in TUNE_KEYS})
         err = ctypes.create_string_buffer(512)
         h = self._lib.gspec_create(ctypes.byref(cfg), err, len(err))
         if not h:
@@ -330,6 +339,16 @@ class GatedSpectrometer:
 
     def last_error(self) -> str:
         return self._lib.gspec_last_error(self._h).decode()
+
+
+def query(config: GspecConfig) -> GspecInfo:
+    """Sizes of a handle for ``config`` (``gspec_query``) without creating it."""
+    lib = load_library()
+    info = GspecInfo()
+    err = ctypes.create_string_buffer(512)
+    if lib.gspec_query(ctypes.byref(config), ctypes.byref(info), err, len(err)) != GSPEC_OK:
+        raise GspecError(err.value.decode())
+    return info
 
 
 def process_block_noalloc(config: GspecConfig, d_block: int, d_baselines: int, d_out: int, stream: int = 0) -> None:

@@ -57,6 +57,7 @@ class StreamSpec:
     selected_bit: int = 0
     diode_period_heaps: int = 32   # diode bit toggles every this many heaps (per pol)
     gap_bytes: int = 0
+    sigma: float = 0.0             # Gaussian sigma of the "default" samples (0: 15 % of full scale)
 
     @property
     def heaps_per_pol(self) -> int:
@@ -96,6 +97,30 @@ def config3() -> StreamSpec:
                       diode_period_heaps=64)
 
 
+def uneven_streams(n: int = 16, seed: int = 3, min_log_block: int = 22, max_log_block: int = 26,
+                   max_log_fft: int = 18) -> list:
+    """Independent streams of mixed shapes (batched-streams workload): fft
+    log-uniform in 2^10..2^max_log_fft, nbits from {8, 10, 12}, naccumulate a
+    power of two in 8..256, block 2^min_log_block..2^max_log_block samples per
+    pol (at least one fft), diode period 16..128 heaps, sigma 10..400 (clipped
+    to the bit depth), single or dual pol.  Heaps hold 4096 samples."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        nbits = int(rng.choice([8, 10, 12]))
+        log_fft = int(rng.integers(10, max_log_fft + 1))
+        log_block = int(rng.integers(max(min_log_block, log_fft), max(max_log_block, log_fft) + 1))
+        nacc = int(1 << rng.integers(3, 9))
+        dual = bool(rng.integers(0, 2))
+        period = int(rng.integers(16, 129))
+        sigma = float(min(rng.uniform(10.0, 400.0), 0.3 * (1 << (nbits - 1))))
+        heap = 4096 * nbits // 8
+        name = f"s{i}_{'dual' if dual else 'single'}_{nbits}bit_fft{1 << log_fft}_nacc{nacc}_blk{1 << log_block}"
+        out.append(StreamSpec(name, nbits, dual, heap, 1, 1 << log_block, 1 << log_fft, nacc,
+                              diode_period_heaps=period, sigma=sigma))
+    return out
+
+
 def _clip(x, nbits):
     lo, hi = -(1 << (nbits - 1)), (1 << (nbits - 1)) - 1
     return np.clip(np.rint(x), lo, hi).astype(np.int32)
@@ -131,7 +156,7 @@ def config_samples(spec: StreamSpec, rng: np.random.Generator, kind: str = "defa
             x[out] = np.where(rng.random(int(out.sum())) < 0.5, -2047.0, 2047.0)
             pols.append(_clip(x, nb))
         return pols
-    sigma = 0.15 * (1 << (nb - 1))
+    sigma = spec.sigma if spec.sigma > 0 else 0.15 * (1 << (nb - 1))
     return [_clip(rng.normal(0.0, sigma, n), nb) for _ in range(spec.npol)]
 
 
