@@ -1,6 +1,6 @@
 """Throughput benchmark of the GB300 gated spectrometer.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c2|c1|c3] [--impl gb300|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c2|c1|c3|c4|c5] [--impl gb300|reference]
 
 One step = one DADA block of the workload through the whole chain (unpack,
 gate, R2C, Stokes/power accumulate).  Default workload: dual-pol 12-bit gated
@@ -8,9 +8,9 @@ Stokes, fft 2^16, naccumulate 32, 2^26 samples per pol per block.
 
 * ``value``   device throughput, input Gsamples/s (both pols), inputs resident
               in HBM: K blocks through gspec_run_block_device on the stream
-              the kernels run on, timed with CUDA events.  Two distinct
-              201 MB blocks alternate, so every step reads inputs larger than
-              L2.
+              the kernels run on, timed with CUDA events.  Distinct device
+              copies of the block rotate, at least 3x the L2 size per
+              rotation, so every step reads its input from HBM.
 * ``e2e``     the same metric through the public handler API
               (GatedSpectrometer.__call__ -> gspec_process) with blocks in
               pinned host memory: every step copies its block host->device and
@@ -25,6 +25,11 @@ CPU implementation of its own, and its GPU chain needs libpsrdada, Boost and
 cuFFT, none of which is installed) on the same metric, each step one output spectrum's worth of
 input.  Under torchrun every rank runs its own stream on its own GPU
 (replicas, weak scaling); rank 0 prints the line.
+
+``--workload c4`` times 16 uneven streams as one CUDA graph per step (and the
+same members without the graph, and end to end from pinned host memory);
+``--workload c5`` runs the serving loop: 32 mixed streams, a peak-rate burst,
+then Poisson arrivals at 60 % of that rate, with block-to-spectrum latency.
 """
 from __future__ import annotations
 
@@ -403,6 +408,195 @@ def run_gpu(args):
         print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------- batched uneven streams
+def run_batch(args):
+    """16 uneven streams (synth.uneven_streams, seed 3) as one CUDA graph per
+    step: every member processes one device-resident block per step.  Also
+    times the same members one after another without the graph, and end to
+    end with the blocks copied from pinned host memory every step."""
+    import torch
+    ws, rank = dist_init("nccl")
+    _, _, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    import psrdada_cpp_gb300 as G
+    from psrdada_cpp_gb300 import synth, autotune
+    specs = synth.uneven_streams(16, seed=3)
+    t_tune = time.time()
+    tunes = {s.name: ({} if args.no_tune else autotune.tune(s, device=local, steps=4)) for s in specs}
+    t_tune = time.time() - t_tune
+    host = [synth.make_block(s, seed=7 + rank, block_index=0) for s in specs]
+    samples_per_step = sum(s.samples_per_pol * s.npol for s in specs)
+    in_bytes = sum(s.buffer_size for s in specs)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+    bt = G.Batch([G.make_config(s, device=local, tune=tunes[s.name]) for s in specs])
+    for i, h in enumerate(host):
+        bt.set_input(i, h, sp)
+    torch.cuda.synchronize(dev)
+    for _ in range(args.warmup):
+        bt.run(sp)
+    torch.cuda.synchronize(dev)
+    steps = args.steps
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    dist_barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    tw0 = time.time()
+    e0.record(stream)
+    for _ in range(steps):
+        bt.run(sp)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    tw1 = time.time()
+    dist_barrier()
+    clocks.stop()
+    ms = dist_max(e0.elapsed_time(e1), dev)
+    value = dist_sum(samples_per_step * steps, dev) / (ms / 1e3) / 1e9
+    kernels = bt.kernels_per_step()
+
+    # the same members one after another, no graph
+    seq = []
+    d_out = []
+    for i, s in enumerate(specs):
+        lay = G.DadaBufferLayout(s.buffer_size, s.heap_size, s.n_side_channels)
+        g = G.GatedSpectrometer(lay, 0, 0, s.fft_length, s.naccumulate, s.nbits, 1.0, 1.0, G.NullSink(),
+                                input_type=G.DUAL_POL if s.dual_pol else G.SINGLE_POL, device=local,
+                                flags=G.FLAG_NO_HOST_BUFFERS, tune=tunes[s.name])
+        seq.append(g)
+        d_out.append(torch.zeros(int(g.info().output_bytes), dtype=torch.uint8, device=dev))
+    d_in = [torch.from_numpy(h).to(dev) for h in host]
+    ks = max(4, steps // 4)
+    for _ in range(2):
+        for g, di, do in zip(seq, d_in, d_out):
+            g.run_block_device(di.data_ptr(), do.data_ptr(), sp)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    for _ in range(ks):
+        for g, di, do in zip(seq, d_in, d_out):
+            g.run_block_device(di.data_ptr(), do.data_ptr(), sp)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    seq_value = samples_per_step * ks / (e0.elapsed_time(e1) / 1e3) / 1e9
+    for g in seq:
+        g.close()
+    del d_in, d_out
+
+    # end to end: pinned host blocks in, completed outputs out, every step
+    pinned = []
+    for h in host:
+        t = torch.empty(h.size, dtype=torch.uint8, pin_memory=True)
+        t.numpy()[:] = h
+        pinned.append(t)
+    outs = [torch.empty(int(bt.info(i).output_bytes), dtype=torch.uint8, pin_memory=True) for i in range(bt.n)]
+    ke = max(4, min(steps, 64))
+    d2h = 0
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        for i, p in enumerate(pinned):
+            bt.set_input(i, p, sp)
+        bt.run(sp)
+        for i in range(bt.n):
+            ptr, n, complete = bt.output(i)
+            if complete:
+                bt._lib.gspec_batch_read_output(bt._b, i, __import__("ctypes").c_void_p(outs[i].data_ptr()), n,
+                                                __import__("ctypes").c_void_p(sp))
+                d2h += n
+    torch.cuda.synchronize(dev)
+    e2e_s = time.perf_counter() - t0
+    bt.close()
+    if rank == 0:
+        line = {
+            "metric": "batched uneven streams: input Gsamples/s (16 streams, one CUDA graph per step)",
+            "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": steps, "warmup": args.warmup,
+            "ms_per_step": round(ms / steps, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "uneven_streams_16_seed3", "streams": [s.name for s in specs],
+                       "samples_per_step": samples_per_step, "input_bytes_per_step": in_bytes, "form": "fp32",
+                       "schedules": tunes, "tune_seconds": round(t_tune, 1),
+                       "l2": "inputs larger than L2: the 16 members' blocks total %d B" % in_bytes},
+            "sequential_no_graph": {"value": round(seq_value, 3), "unit": UNIT, "steps": ks},
+            "e2e": {"value": round(samples_per_step * ke / e2e_s / 1e9, 3), "unit": UNIT,
+                    "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": int(d2h / ke), "steps": ke,
+                    "api": "Batch.set_input (pinned) -> gspec_batch_run -> gspec_batch_read_output"},
+            "gpu_launches": int(kernels * steps), "kernels_per_graph": int(kernels),
+            "clocks": clocks.summary(tw0, tw1),
+        }
+        print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------- serving loop
+def run_serve(args):
+    """32 virtual streams (16 of the 8-bit fft-1024 shape, 16 of the dual-pol
+    12-bit fft-2^20 shape) through one Server: first every block of an
+    equal-samples-per-stream workload at once (peak aggregate rate), then
+    Poisson arrivals at 60 % of that rate until args.serve_blocks blocks."""
+    # every served stream drives three CUDA streams; give them their own
+    # hardware work queues (the default of 8 shares queues between streams,
+    # so a short block can wait behind another stream's long kernels)
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", str(args.connections))
+    import torch
+    ws, rank = dist_init("nccl")
+    _, _, local = dist_env()
+    torch.cuda.set_device(local)
+    import psrdada_cpp_gb300 as G
+    from psrdada_cpp_gb300 import synth, loadgen, autotune
+    c1, c3 = synth.config1(), synth.config3()
+    specs = [c1] * 16 + [c3] * 16
+    tunes = {} if args.no_tune else {s.name: autotune.tune(s, device=local, steps=4) for s in (c1, c3)}
+
+    def pinned(arr):
+        t = torch.empty(arr.size, dtype=torch.uint8, pin_memory=True)
+        t.numpy()[:] = arr
+        return t
+
+    host = {c1.name: [pinned(synth.make_block(c1, seed=4, block_index=i, kind="c1")) for i in range(2)],
+            c3.name: [pinned(synth.make_block(c3, seed=4, block_index=0, kind="c3"))]}
+    budget = int(args.budget_gb * 2**30)
+    ratio = (c3.samples_per_pol * c3.npol) // (c1.samples_per_pol * c1.npol)
+    m = args.serve_peak_blocks
+    burst = loadgen.burst_plan(specs, [m * ratio] * 16 + [m] * 16)
+    prios = {} if args.no_priority else loadgen.span_priorities(specs)
+    infl = int(args.inflight_gb * 2**30)
+    peak = loadgen.run(specs, host, burst, budget, device=local, tunes=tunes, priorities=prios, inflight_bytes=infl)
+    rate = 0.6 * peak["gsamples_per_s"] * 1e9 / len(specs)
+    plan = loadgen.poisson_plan(specs, rate, args.serve_blocks, seed=4)
+    clocks = ClockSampler(local)
+    clocks.start()
+    tw0 = time.time()
+    res = loadgen.run(specs, host, plan, budget, device=local, tunes=tunes, priorities=prios, inflight_bytes=infl)
+    tw1 = time.time()
+    clocks.stop()
+    lat = loadgen.latency_summary(res, specs, rate)
+    if rank == 0:
+        worst = max(v["p99_over_span"] for v in lat["by_shape"].values())
+        line = {
+            "metric": "serving: input Gsamples/s and p50/p95/p99 block-to-spectrum latency (32 mixed streams)",
+            "value": round(res["gsamples_per_s"], 3), "unit": UNIT, "n_gpus": ws, "steps": int(lat["blocks"]),
+            "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "serving_32_streams_c1x16_c3x16", "arrivals": "Poisson, seed 4",
+                       "offered_rate_gsps": round(0.6 * peak["gsamples_per_s"], 3),
+                       "peak_gsps": round(peak["gsamples_per_s"], 3), "peak_blocks": len(burst),
+                       "memory_budget_bytes": budget, "inflight_bytes": infl, "schedules": tunes,
+                       "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
+                       "stream_priorities": prios,
+                       "form": "fp32"},
+            "latency_ms": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in lat.items()
+                           if k != "by_shape"},
+            "latency_by_shape": {k: {kk: round(vv, 4) if isinstance(vv, float) else vv for kk, vv in v.items()}
+                                 for k, v in lat["by_shape"].items()},
+            "worst_p99_over_block_span": round(worst, 4),
+            "elapsed_s": round(res["elapsed_s"], 3), "gpu_launches": int(res["launches"]),
+            "e2e": {"value": round(res["gsamples_per_s"], 3), "unit": UNIT,
+                    "api": "Server.submit (pinned host blocks) -> gspec_poll (spectra on the host)"},
+            "clocks": clocks.summary(tw0, tw1),
+        }
+        print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------- reference arm
 def run_reference(args):
     ws, rank, _ = dist_env()
@@ -454,16 +648,28 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["c1", "c2", "c3"], default="c2")
+    ap.add_argument("--workload", choices=["c1", "c2", "c3", "c4", "c5"], default="c2",
+                    help="c1-c3 one stream; c4 16 uneven streams in one CUDA graph; c5 the serving loop")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-budget-s", type=float, default=150.0)
+    ap.add_argument("--no-tune", action="store_true", help="c4/c5: built-in schedules instead of the autotuner's")
+    ap.add_argument("--serve-blocks", type=int, default=10000, help="c5: blocks of the Poisson phase")
+    ap.add_argument("--serve-peak-blocks", type=int, default=4, help="c5: fft-2^20 blocks per stream, peak phase")
+    ap.add_argument("--budget-gb", type=float, default=120.0, help="c5: device memory budget of the server")
+    ap.add_argument("--no-priority", action="store_true", help="c5: equal CUDA stream priorities")
+    ap.add_argument("--inflight-gb", type=float, default=0.0, help="c5: input bytes on the GPU at once (0: no limit)")
+    ap.add_argument("--connections", type=int, default=32, help="c5: CUDA_DEVICE_MAX_CONNECTIONS")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "c4":
+        run_batch(args)
+    elif args.workload == "c5":
+        run_serve(args)
     else:
         run_gpu(args)
 

@@ -71,6 +71,10 @@ typedef struct gspec_config {
   uint64_t tune_units;            /* shared-memory path: target work units per block (default 4 x SMs) */
   uint32_t tune_n1;               /* four-step path: first-pass length N1 (N2 = fft_length/N1 in [128, 1024]) */
   uint32_t tune_scratch_mb;       /* four-step path: scratch budget of one chunk of spectra (default 512 MiB) */
+  /* CUDA priority of the handle's streams (0 default; negative = higher,
+   * clamped to the device's range): a server gives latency-critical streams
+   * (short blocks) precedence over long blocks of other streams. */
+  int32_t stream_priority;
 } gspec_config;
 
 typedef struct gspec_info {
@@ -200,6 +204,9 @@ typedef struct gspec_server_config {
   int32_t max_inflight;     /* blocks of one stream on the GPU at once (1 or 2; 0 = 2) */
   int32_t output_buffers;   /* pinned host output buffers per stream (0 = 2) */
   int32_t reserved;
+  uint64_t inflight_bytes;  /* input bytes of all streams' blocks on the GPU at once (0 = no limit); a
+                               block that would exceed it waits unless nothing is in flight.  Bounds
+                               the copy and kernel queues that short blocks wait behind */
 } gspec_server_config;
 typedef struct gspec_result {
   int32_t stream;           /* stream id */
@@ -213,6 +220,10 @@ typedef struct gspec_result {
   double t_submit;          /* seconds on the server clock: gspec_submit called */
   double t_start;           /* the block's first copy was issued to the GPU */
   double t_done;            /* output on the host (or the block finished) */
+  /* GPU-side stages of the block from CUDA events, in ms: the input copy,
+   * the wait between copy and chain (earlier blocks of the stream, the
+   * output accumulator), the chain's kernels, and the output copy. */
+  float h2d_ms, wait_ms, chain_ms, d2h_ms;
 } gspec_result;
 gspec_server* gspec_server_create(const gspec_server_config* cfg, char* err, size_t err_len);
 /* Waits for the streams' outstanding blocks, then frees everything. */

@@ -188,8 +188,9 @@ cudaError_t timed(gspec_handle* h, int kind, cudaStream_t s, F&& launch) {
 // Copies the device error word to its pinned host mirror behind the block's
 // kernels (no copy when the caller supplied no mirror).
 cudaError_t refresh_error_word(gspec_handle* h, cudaStream_t s) {
-  if (!h->h_err || !h->d_err) return cudaSuccess;
-  return cudaMemcpyAsync(h->h_err, h->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+  if (!h->h_err_dev || !h->d_err) return cudaSuccess;
+  ++h->launches;
+  return launch_mirror_word(h->d_err, h->h_err_dev, s);
 }
 
 // Error status of the kernels that completed so far.
@@ -503,9 +504,14 @@ gspec_handle* gspec_create(const gspec_config* cfg, char* err, size_t err_len) {
   };
   if (cudaSetDevice(cfg->device) != cudaSuccess) return bail("cudaSetDevice failed");
   if (!gspec_engine::plan_handle(h)) return bail("");
-  if (!cuda_ok(h, cudaStreamCreateWithFlags(&h->h2d, cudaStreamNonBlocking), "stream") ||
-      !cuda_ok(h, cudaStreamCreateWithFlags(&h->proc, cudaStreamNonBlocking), "stream") ||
-      !cuda_ok(h, cudaStreamCreateWithFlags(&h->d2h, cudaStreamNonBlocking), "stream"))
+  int least = 0, greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  int prio = cfg->stream_priority;
+  if (prio > least) prio = least;
+  if (prio < greatest) prio = greatest;
+  if (!cuda_ok(h, cudaStreamCreateWithPriority(&h->h2d, cudaStreamNonBlocking, prio), "stream") ||
+      !cuda_ok(h, cudaStreamCreateWithPriority(&h->proc, cudaStreamNonBlocking, prio), "stream") ||
+      !cuda_ok(h, cudaStreamCreateWithPriority(&h->d2h, cudaStreamNonBlocking, prio), "stream"))
     return bail("");
   for (int i = 0; i < 2; ++i) {
     if (!cuda_ok(h, cudaEventCreateWithFlags(&h->ev_h2d[i], cudaEventDisableTiming), "event") ||
@@ -541,6 +547,9 @@ gspec_handle* gspec_create(const gspec_config* cfg, char* err, size_t err_len) {
       !cuda_ok(h, cudaMallocHost(reinterpret_cast<void**>(&h->h_err), sizeof(uint32_t)), "pinned error word"))
     return bail("");
   *h->h_err = 0;
+  if (!cuda_ok(h, cudaHostGetDevicePointer(reinterpret_cast<void**>(&h->h_err_dev), h->h_err, 0),
+               "device address of the error word"))
+    return bail("");
   cudaMemset(h->d_err, 0, sizeof(uint32_t));
   if (h->path == 0) {
     if (!dalloc(h, &h->d_tw, tw_size(N) * sizeof(float2), "twiddles")) return bail("");

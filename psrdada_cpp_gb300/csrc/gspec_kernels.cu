@@ -548,4 +548,32 @@ cudaError_t launch_unpack(int nbits, const uint8_t* raw, uint64_t nsamples, floa
   return cudaGetLastError();
 }
 
+// Mirrors the device error word into host memory (page-locked, device
+// accessible) with one store from an SM: no copy engine is involved, so the
+// status of a block never waits behind other streams' bulk copies.
+__global__ void mirror_word_kernel(const uint32_t* __restrict__ src, volatile uint32_t* dst) { *dst = *src; }
+
+cudaError_t launch_mirror_word(const uint32_t* src, uint32_t* dst, cudaStream_t s) {
+  mirror_word_kernel<<<1, 1, 0, s>>>(src, dst);
+  return cudaGetLastError();
+}
+
+// Copies 8-byte words from device memory to page-locked host memory with
+// SM stores (small outputs of the serving loop).
+__global__ void copy_words_kernel(const uint2* __restrict__ src, uint2* dst, uint64_t n) {
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += stride) dst[i] = src[i];
+}
+
+cudaError_t launch_copy_words(void* dst, const void* src, uint64_t bytes, int sm_count, cudaStream_t s) {
+  if (bytes % 8) return cudaErrorInvalidValue;
+  const uint64_t n = bytes / 8;
+  uint64_t blocks = (n + 255) / 256;
+  if (blocks > 2ull * sm_count) blocks = 2ull * sm_count;
+  if (blocks < 1) blocks = 1;
+  copy_words_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(static_cast<const uint2*>(src),
+                                                                 static_cast<uint2*>(dst), n);
+  return cudaGetLastError();
+}
+
 }  // namespace gspec

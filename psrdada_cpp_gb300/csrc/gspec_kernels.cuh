@@ -58,6 +58,10 @@ cudaError_t launch_fourstep_twiddles(int N, float2* twA, float2* twB, cudaStream
 cudaError_t launch_gate_debug(int nbits, const GateParams& g, const float* baselines, int npol, uint32_t nsamps,
                               float* out, cudaStream_t s);
 cudaError_t launch_unpack(int nbits, const uint8_t* raw, uint64_t nsamples, float* out, cudaStream_t s);
+// One store of *src into device-accessible host memory dst.
+cudaError_t launch_mirror_word(const uint32_t* src, uint32_t* dst, cudaStream_t s);
+// bytes (a multiple of 8) from device memory to device-accessible host memory by SM stores.
+cudaError_t launch_copy_words(void* dst, const void* src, uint64_t bytes, int sm_count, cudaStream_t s);
 cudaError_t launch_fourstep(int N, int nbits, bool dual, const FourStepParams& p, int pass, cudaStream_t s);
 // masks of every item; per-frame gate flags when flags != nullptr
 cudaError_t launch_prepass(const GateParams& g, uint32_t nitems, uint8_t* masks, uint32_t N, uint32_t nframes,

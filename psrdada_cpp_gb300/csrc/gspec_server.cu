@@ -10,15 +10,18 @@
 //   * state: each admitted stream keeps its handle (baselines, counters,
 //     output accumulators, twiddles, scratch) resident in device memory;
 //   * continuous batching: a stream's next block is issued as soon as it is
-//     queued, its stream has fewer than max_inflight blocks on the GPU and a
-//     host output buffer is free, so blocks of different streams overlap on
-//     the device in their own CUDA streams;
+//     queued, its stream has fewer than max_inflight blocks on the GPU, the
+//     input bytes on the GPU stay within inflight_bytes and a host output
+//     buffer is free, so blocks of different streams overlap on the device in
+//     their own CUDA streams (streams are scanned in id order each pass);
 //   * completion: each block's last operation records an event; the loop
 //     queries the oldest event of every stream and posts results in order.
 // Per block the work is the handle's chain (gspec_engine::run_chain): H2D on
-// the handle's copy stream into one of two input buffers, the chain on its
-// compute stream into one of two output accumulators, and at the end of an
-// output block the D2H of that accumulator on its copy-out stream.
+// the handle's copy stream (in 8 MiB pieces) into one of two input buffers,
+// the chain on its compute stream into one of two output accumulators, and at
+// the end of an output block the accumulator's way to the host: SM stores
+// into the page-locked result buffer for outputs up to 16 MiB, else a D2H
+// copy (in pieces) on the handle's copy-out stream.
 #include <chrono>
 #include <condition_variable>
 #include <cstdio>
@@ -52,6 +55,8 @@ struct Flight {
   double t_start;
   int obuf;        // host output buffer, -1 when the block completes no output
   cudaEvent_t done;
+  uint64_t bytes;  // input bytes (in-flight limit)
+  int slot;        // event slot of the stage timings
 };
 
 constexpr int kEventsPerStream = 4;
@@ -61,15 +66,18 @@ struct Stream {
   gspec_config cfg{};
   gspec_info info{};
   uint64_t bytes = 0;          // device bytes (admission)
-  int state = 0;               // 0 waiting, 1 admitted, 2 closing, 3 closed
+  int state = 0;               // 0 waiting, 1 admitted, 2 closing, 3 closed, 4 being admitted, 5 being freed
+  bool close_requested = false;
   gspec_handle* h = nullptr;
   std::deque<Queued> queue;
   std::deque<Flight> flight;
   uint64_t submitted = 0;
   uint64_t issued = 0;
   std::vector<char*> hbuf;
+  std::vector<char*> hbuf_dev;   // device addresses of hbuf
   std::vector<int> hfree;
-  cudaEvent_t ev[kEventsPerStream] = {};
+  cudaEvent_t ev[kEventsPerStream] = {};        // block finished
+  cudaEvent_t ev_stage[4][kEventsPerStream] = {};   // copy start, copy end, chain start, chain end
   int ev_next = 0;
   cudaEvent_t ev_out_done[2] = {};   // D2H of output accumulator i finished
   cudaEvent_t ev_out_full[2] = {};   // chain of the last block of output i finished
@@ -88,6 +96,7 @@ struct gspec_server {
   std::deque<int> admit;
   std::deque<gspec_result> results;
   uint64_t in_use = 0;
+  uint64_t inflight_bytes = 0;  // input bytes of the blocks on the GPU
   uint64_t launches_done = 0;   // launches of streams already closed
   bool stop = false;
   std::thread worker;
@@ -111,9 +120,13 @@ void free_stream_memory(Stream& st) {
   for (char* p : st.hbuf)
     if (p) cudaFreeHost(p);
   st.hbuf.clear();
+  st.hbuf_dev.clear();
   st.hfree.clear();
   for (auto& e : st.ev)
     if (e) cudaEventDestroy(e), e = nullptr;
+  for (auto& row : st.ev_stage)
+    for (auto& e : row)
+      if (e) cudaEventDestroy(e), e = nullptr;
   for (int i = 0; i < 2; ++i) {
     if (st.ev_out_done[i]) cudaEventDestroy(st.ev_out_done[i]), st.ev_out_done[i] = nullptr;
     if (st.ev_out_full[i]) cudaEventDestroy(st.ev_out_full[i]), st.ev_out_full[i] = nullptr;
@@ -122,25 +135,51 @@ void free_stream_memory(Stream& st) {
   st.h = nullptr;
 }
 
-// Creates the handle and host buffers of an admitted stream (worker thread).
-bool admit_stream(gspec_server* s, Stream& st) {
+// Moves the GPU resources (handle, events, host buffers) from src to dst.
+void take_resources(Stream& dst, Stream& src) {
+  dst.h = src.h;
+  src.h = nullptr;
+  dst.info = src.info;
+  dst.hbuf.swap(src.hbuf);
+  dst.hbuf_dev.swap(src.hbuf_dev);
+  dst.hfree.swap(src.hfree);
+  for (int i = 0; i < kEventsPerStream; ++i) {
+    std::swap(dst.ev[i], src.ev[i]);
+    for (int k = 0; k < 4; ++k) std::swap(dst.ev_stage[k][i], src.ev_stage[k][i]);
+  }
+  for (int i = 0; i < 2; ++i) {
+    std::swap(dst.ev_out_done[i], src.ev_out_done[i]);
+    std::swap(dst.ev_out_full[i], src.ev_out_full[i]);
+  }
+}
+
+// Creates the handle and host buffers of an admitted stream into st (called
+// by the worker without the server lock: pinning host memory and allocating
+// device memory take milliseconds to seconds).
+bool admit_stream(const gspec_server_config& scfg, const gspec_config& cfg, int id, Stream& st, std::string& err) {
   char msg[256] = {0};
-  gspec_config c = st.cfg;
-  c.device = s->cfg.device;
+  gspec_config c = cfg;
+  c.device = scfg.device;
   c.flags |= GSPEC_FLAG_NO_HOST_BUFFERS;
   st.h = gspec_create(&c, msg, sizeof(msg));
   if (!st.h) {
-    s->err = std::string("stream ") + std::to_string(st.id) + ": " + msg;
+    err = std::string("stream ") + std::to_string(id) + ": " + msg;
     return false;
   }
   gspec_get_info(st.h, &st.info);
-  const int nb = s->cfg.output_buffers > 0 ? s->cfg.output_buffers : 2;
+  const int nb = scfg.output_buffers > 0 ? scfg.output_buffers : 2;
   st.hbuf.assign(nb, nullptr);
+  st.hbuf_dev.assign(nb, nullptr);
   st.hfree.assign(nb, 1);
   for (int i = 0; i < nb; ++i)
-    if (cudaMallocHost(reinterpret_cast<void**>(&st.hbuf[i]), st.info.output_bytes) != cudaSuccess) return false;
+    if (cudaMallocHost(reinterpret_cast<void**>(&st.hbuf[i]), st.info.output_bytes) != cudaSuccess ||
+        cudaHostGetDevicePointer(reinterpret_cast<void**>(&st.hbuf_dev[i]), st.hbuf[i], 0) != cudaSuccess)
+      return false;
   for (auto& e : st.ev)
-    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return false;
+    if (cudaEventCreate(&e) != cudaSuccess) return false;
+  for (auto& row : st.ev_stage)
+    for (auto& e : row)
+      if (cudaEventCreate(&e) != cudaSuccess) return false;
   for (int i = 0; i < 2; ++i) {
     if (cudaEventCreateWithFlags(&st.ev_out_done[i], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&st.ev_out_full[i], cudaEventDisableTiming) != cudaSuccess)
@@ -151,6 +190,26 @@ bool admit_stream(gspec_server* s, Stream& st) {
   return true;
 }
 
+// Large copies go out in pieces: the copy engines take work from the streams
+// of all served streams piece by piece, so a short block's copy waits for at
+// most one piece of a long block's copy instead of the whole of it.
+constexpr size_t kCopyPiece = 8u << 20;
+
+cudaError_t copy_pieces(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t s) {
+  auto* d = static_cast<char*>(dst);
+  auto* p = static_cast<const char*>(src);
+  for (size_t off = 0; off < bytes; off += kCopyPiece) {
+    const size_t n = bytes - off < kCopyPiece ? bytes - off : kCopyPiece;
+    const cudaError_t e = cudaMemcpyAsync(d + off, p + off, n, kind, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// Outputs up to this size reach the host by SM stores on the compute stream
+// (no copy engine: they never queue behind other streams' bulk copies).
+constexpr uint64_t kStoreCopyMax = 16u << 20;
+
 // Enqueues one block of an admitted stream on its handle's streams.
 bool issue(gspec_server* s, Stream& st, const Queued& q, int obuf) {
   gspec_handle* h = st.h;
@@ -159,11 +218,14 @@ bool issue(gspec_server* s, Stream& st, const Queued& q, int obuf) {
   const int oi = static_cast<int>((q.index / nb) & 1);
   const bool first = q.index % nb == 0;
   const bool last = obuf >= 0;
-  Flight f{q.index, q.tag, q.t_submit, now_s(s), obuf, st.ev[st.ev_next]};
+  const int es = st.ev_next;
+  Flight f{q.index, q.tag, q.t_submit, now_s(s), obuf, st.ev[es], q.size, es};
   st.ev_next = (st.ev_next + 1) % kEventsPerStream;
   if (!ok(st, cudaStreamWaitEvent(h->h2d, h->ev_in_free[slot], 0), "wait input") ||
-      !ok(st, cudaMemcpyAsync(h->d_in[slot], q.data, q.size, cudaMemcpyDefault, h->h2d), "H2D block") ||
+      !ok(st, cudaEventRecord(st.ev_stage[0][es], h->h2d), "record") ||
+      !ok(st, copy_pieces(h->d_in[slot], q.data, q.size, cudaMemcpyDefault, h->h2d), "H2D block") ||
       !ok(st, cudaEventRecord(h->ev_h2d[slot], h->h2d), "record") ||
+      !ok(st, cudaEventRecord(st.ev_stage[1][es], h->h2d), "record") ||
       !ok(st, cudaStreamWaitEvent(h->proc, h->ev_h2d[slot], 0), "wait H2D"))
     return false;
   if (first) {
@@ -173,17 +235,28 @@ bool issue(gspec_server* s, Stream& st, const Queued& q, int obuf) {
         !ok(st, cudaMemsetAsync(h->d_sat[oi], 0, h->ext_bytes, h->proc), "clear saturation"))
       return false;
   }
-  if (!ok(st, gspec_engine::run_chain(h, h->d_in[slot], h->d_out[oi], h->d_sat[oi], h->proc), "chain") ||
-      !ok(st, cudaEventRecord(h->ev_in_free[slot], h->proc), "record"))
+  if (!ok(st, cudaEventRecord(st.ev_stage[2][es], h->proc), "record") ||
+      !ok(st, gspec_engine::run_chain(h, h->d_in[slot], h->d_out[oi], h->d_sat[oi], h->proc), "chain") ||
+      !ok(st, cudaEventRecord(h->ev_in_free[slot], h->proc), "record") ||
+      !ok(st, cudaEventRecord(st.ev_stage[3][es], h->proc), "record"))
     return false;
-  if (last) {
+  const bool sat = (st.cfg.flags & GSPEC_FLAG_SATURATION_RECORD) != 0;
+  if (last && h->out_bytes + (sat ? h->ext_bytes : 0) <= kStoreCopyMax) {
+    char* dst = st.hbuf_dev[obuf];
+    if (!ok(st, gspec::launch_copy_words(dst, h->d_out[oi], h->out_bytes, h->sm_count, h->proc), "output copy") ||
+        (sat && !ok(st, gspec::launch_copy_words(dst + h->out_bytes, h->d_sat[oi], h->ext_bytes, h->sm_count, h->proc),
+                    "saturation copy")) ||
+        !ok(st, cudaEventRecord(st.ev_out_done[oi], h->proc), "record") ||
+        !ok(st, cudaEventRecord(f.done, h->proc), "record"))
+      return false;
+    h->launches += sat ? 2 : 1;
+  } else if (last) {
     char* dst = st.hbuf[obuf];
     if (!ok(st, cudaEventRecord(st.ev_out_full[oi], h->proc), "record") ||
         !ok(st, cudaStreamWaitEvent(h->d2h, st.ev_out_full[oi], 0), "wait output") ||
-        !ok(st, cudaMemcpyAsync(dst, h->d_out[oi], h->out_bytes, cudaMemcpyDeviceToHost, h->d2h), "D2H output"))
+        !ok(st, copy_pieces(dst, h->d_out[oi], h->out_bytes, cudaMemcpyDeviceToHost, h->d2h), "D2H output"))
       return false;
-    if ((st.cfg.flags & GSPEC_FLAG_SATURATION_RECORD) &&
-        !ok(st, cudaMemcpyAsync(dst + h->out_bytes, h->d_sat[oi], h->ext_bytes, cudaMemcpyDeviceToHost, h->d2h),
+    if (sat && !ok(st, cudaMemcpyAsync(dst + h->out_bytes, h->d_sat[oi], h->ext_bytes, cudaMemcpyDeviceToHost, h->d2h),
             "D2H saturation"))
       return false;
     if (!ok(st, cudaEventRecord(st.ev_out_done[oi], h->d2h), "record") ||
@@ -193,6 +266,7 @@ bool issue(gspec_server* s, Stream& st, const Queued& q, int obuf) {
     if (!ok(st, cudaEventRecord(f.done, h->proc), "record")) return false;
   }
   ++st.issued;
+  s->inflight_bytes += f.bytes;
   st.flight.push_back(f);
   return true;
 }
@@ -209,6 +283,16 @@ gspec_result make_result(const Stream& st, const Flight& f, int status, double t
   r.t_submit = f.t_submit;
   r.t_start = f.t_start;
   r.t_done = t_done;
+  if (f.done && f.slot >= 0 && status == GSPEC_OK) {
+    auto ms = [](cudaEvent_t a, cudaEvent_t b) {
+      float v = 0.f;
+      return cudaEventElapsedTime(&v, a, b) == cudaSuccess ? v : -1.f;
+    };
+    r.h2d_ms = ms(st.ev_stage[0][f.slot], st.ev_stage[1][f.slot]);
+    r.wait_ms = ms(st.ev_stage[1][f.slot], st.ev_stage[2][f.slot]);
+    r.chain_ms = ms(st.ev_stage[2][f.slot], st.ev_stage[3][f.slot]);
+    r.d2h_ms = ms(st.ev_stage[3][f.slot], f.done);
+  }
   return r;
 }
 
@@ -225,22 +309,34 @@ void worker_loop(gspec_server* s) {
   std::unique_lock<std::mutex> lk(s->mu);
   for (;;) {
     bool progress = false;
-    // admission, FIFO
+    // admission, FIFO; the allocations run without the lock
     while (!s->admit.empty()) {
       Stream& st = *s->streams[s->admit.front()];
       if (s->in_use + st.bytes > s->cfg.memory_budget) break;
       s->admit.pop_front();
       s->in_use += st.bytes;
-      if (!admit_stream(s, st)) {
+      st.state = 4;
+      const gspec_config cfg = st.cfg;
+      const int id = st.id;
+      Stream fresh;
+      std::string aerr;
+      lk.unlock();
+      const bool good = admit_stream(s->cfg, cfg, id, fresh, aerr);
+      lk.lock();
+      take_resources(st, fresh);
+      if (!good) {
         st.failed = true;
-        if (st.h && s->err.empty()) s->err = st.h->err;
+        if (s->err.empty()) s->err = aerr;
       }
-      st.state = st.state == 2 ? 2 : 1;
+      st.state = st.close_requested ? 2 : 1;
       progress = true;
+      lk.unlock();
+      free_stream_memory(fresh);   // whatever a failed admission left behind
+      lk.lock();
     }
     bool busy = false;
-    for (auto& up : s->streams) {
-      Stream& st = *up;
+    for (size_t k = 0; k < s->streams.size(); ++k) {
+      Stream& st = *s->streams[k];
       if (st.state != 1 && st.state != 2) continue;
       // completions, in order
       while (!st.flight.empty()) {
@@ -258,6 +354,7 @@ void worker_loop(gspec_server* s) {
           st.failed = true;
         }
         s->results.push_back(make_result(st, f, status, now_s(s)));
+        s->inflight_bytes -= f.bytes;
         st.flight.pop_front();
         progress = true;
         s->cv_result.notify_all();
@@ -266,13 +363,15 @@ void worker_loop(gspec_server* s) {
       while (!st.queue.empty() && static_cast<int>(st.flight.size()) < max_inflight) {
         const Queued& q = st.queue.front();
         if (st.failed || !st.h) {
-          Flight f{q.index, q.tag, q.t_submit, now_s(s), -1, nullptr};
+          Flight f{q.index, q.tag, q.t_submit, now_s(s), -1, nullptr, 0, -1};
           s->results.push_back(make_result(st, f, GSPEC_ERR_STATE, now_s(s)));
           st.queue.pop_front();
           s->cv_result.notify_all();
           progress = true;
           continue;
         }
+        if (s->cfg.inflight_bytes && s->inflight_bytes > 0 && s->inflight_bytes + q.size > s->cfg.inflight_bytes)
+          break;   // the GPU holds enough work: wait for a block to finish
         int obuf = -1;
         if ((q.index + 1) % st.info.n_blocks == 0) {
           for (size_t i = 0; i < st.hfree.size(); ++i)
@@ -293,7 +392,12 @@ void worker_loop(gspec_server* s) {
       if (!st.flight.empty()) busy = true;
       if (st.state == 2 && stream_idle(st)) {
         if (st.h) s->launches_done += st.h->launches;
-        free_stream_memory(st);
+        st.state = 5;
+        Stream gone;
+        take_resources(gone, st);
+        lk.unlock();
+        free_stream_memory(gone);
+        lk.lock();
         s->in_use -= st.bytes;
         st.state = 3;
         progress = true;
@@ -302,8 +406,7 @@ void worker_loop(gspec_server* s) {
     if (s->stop) {
       bool all_idle = true;
       for (auto& up : s->streams)
-        if (up->state == 1 || up->state == 2 || up->state == 0)
-          if (!up->queue.empty() || !up->flight.empty()) all_idle = false;
+        if (up->state != 3 && (!up->queue.empty() || !up->flight.empty())) all_idle = false;
       if (all_idle) break;
     }
     if (!progress) {
@@ -395,7 +498,8 @@ int gspec_stream_state(gspec_server* s, int stream_id) {
   if (!s) return GSPEC_ERR_ARG;
   std::lock_guard<std::mutex> lk(s->mu);
   Stream* st = find(s, stream_id);
-  return st ? st->state : GSPEC_ERR_ARG;
+  if (!st) return GSPEC_ERR_ARG;
+  return st->state == 4 ? 0 : (st->state == 5 ? 2 : st->state);
 }
 
 int gspec_submit(gspec_server* s, int stream_id, const void* block, size_t size, uint64_t tag) {
@@ -403,7 +507,7 @@ int gspec_submit(gspec_server* s, int stream_id, const void* block, size_t size,
   const double t = now_s(s);
   std::lock_guard<std::mutex> lk(s->mu);
   Stream* st = find(s, stream_id);
-  if (!st || st->state >= 2) {
+  if (!st || st->state == 2 || st->state == 3 || st->state == 5 || st->close_requested) {
     s->err = "unknown or closed stream";
     return GSPEC_ERR_ARG;
   }
@@ -468,6 +572,7 @@ int gspec_stream_close(gspec_server* s, int stream_id) {
     s->cv_result.notify_all();
     return GSPEC_OK;
   }
+  if (st->state == 4) st->close_requested = true;
   if (st->state == 1) st->state = 2;
   s->cv_work.notify_all();
   return GSPEC_OK;

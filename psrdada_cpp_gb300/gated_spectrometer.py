@@ -52,6 +52,7 @@ class GspecConfig(ctypes.Structure):
         ("tune_units", ctypes.c_uint64),
         ("tune_n1", ctypes.c_uint32),
         ("tune_scratch_mb", ctypes.c_uint32),
+        ("stream_priority", ctypes.c_int32),
     ]
 
 

@@ -20,14 +20,16 @@ from .gated_spectrometer import (GspecConfig, GspecError, GspecInfo, DUAL_POL, F
 
 class GspecServerConfig(ctypes.Structure):
     _fields_ = [("memory_budget", ctypes.c_uint64), ("device", ctypes.c_int32), ("max_inflight", ctypes.c_int32),
-                ("output_buffers", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("output_buffers", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("inflight_bytes", ctypes.c_uint64)]
 
 
 class GspecResult(ctypes.Structure):
     _fields_ = [("stream", ctypes.c_int32), ("status", ctypes.c_int32), ("tag", ctypes.c_uint64),
                 ("block_index", ctypes.c_uint64), ("data", ctypes.c_void_p), ("size", ctypes.c_uint64),
                 ("buffer", ctypes.c_int32), ("reserved", ctypes.c_int32), ("t_submit", ctypes.c_double),
-                ("t_start", ctypes.c_double), ("t_done", ctypes.c_double)]
+                ("t_start", ctypes.c_double), ("t_done", ctypes.c_double), ("h2d_ms", ctypes.c_float),
+                ("wait_ms", ctypes.c_float), ("chain_ms", ctypes.c_float), ("d2h_ms", ctypes.c_float)]
 
 
 def declare(lib) -> None:
@@ -73,9 +75,10 @@ def declare(lib) -> None:
 
 
 def make_config(spec, device: int = 0, flags: int = 0, tune: dict | None = None,
-                convention: int = INTENDED) -> GspecConfig:
-    """``GspecConfig`` of a ``synth.StreamSpec`` (selected side channel/bit, layout, shape)."""
-    return GspecConfig(
+                convention: int = INTENDED, priority: int = 0) -> GspecConfig:
+    """``GspecConfig`` of a ``synth.StreamSpec`` (selected side channel/bit, layout, shape);
+    ``priority`` is the CUDA stream priority (negative = higher)."""
+    return GspecConfig(stream_priority=priority,
         buffer_size=spec.buffer_size, heap_size=spec.heap_size, n_side_channels=spec.n_side_channels,
         selected_side_channel=spec.selected_side_channel, selected_bit=spec.selected_bit,
         fft_length=spec.fft_length, naccumulate=spec.naccumulate, nbits=spec.nbits,
@@ -94,10 +97,11 @@ class Server:
     finished results as dicts, copying each output block out and releasing
     its buffer (``copy=False`` keeps the buffer until ``release``)."""
 
-    def __init__(self, memory_budget: int, device: int = 0, max_inflight: int = 2, output_buffers: int = 2):
+    def __init__(self, memory_budget: int, device: int = 0, max_inflight: int = 2, output_buffers: int = 2,
+                 inflight_bytes: int = 0):
         self._lib = load_library()
         cfg = GspecServerConfig(memory_budget=int(memory_budget), device=device, max_inflight=max_inflight,
-                                output_buffers=output_buffers)
+                                output_buffers=output_buffers, inflight_bytes=int(inflight_bytes))
         err = ctypes.create_string_buffer(512)
         s = self._lib.gspec_server_create(ctypes.byref(cfg), err, len(err))
         if not s:
@@ -160,6 +164,7 @@ class Server:
         for r in res[:n]:
             d = {"stream": r.stream, "status": r.status, "tag": r.tag, "block_index": r.block_index,
                  "t_submit": r.t_submit, "t_start": r.t_start, "t_done": r.t_done, "buffer": r.buffer,
+                 "h2d_ms": r.h2d_ms, "wait_ms": r.wait_ms, "chain_ms": r.chain_ms, "d2h_ms": r.d2h_ms,
                  "size": r.size, "data": None}
             if r.data and copy:
                 d["data"] = np.ctypeslib.as_array((ctypes.c_uint8 * r.size).from_address(r.data)).copy()

@@ -18,12 +18,12 @@ ROOT = __import__("pathlib").Path(__file__).resolve().parents[1]
 
 STRUCTS = {
     "gspec_config": (GspecConfig, ["buffer_size", "naccumulate", "nbits", "device", "flags", "tune_units",
-                                   "tune_n1", "tune_scratch_mb"]),
+                                   "tune_n1", "tune_scratch_mb", "stream_priority"]),
     "gspec_info": (GspecInfo, ["nchans", "device_bytes", "kernel_launches"]),
     "gspec_server_config": (serving.GspecServerConfig, ["memory_budget", "device", "max_inflight",
-                                                        "output_buffers"]),
+                                                        "output_buffers", "inflight_bytes"]),
     "gspec_result": (serving.GspecResult, ["stream", "status", "tag", "block_index", "data", "size", "buffer",
-                                           "t_submit", "t_start", "t_done"]),
+                                           "t_submit", "t_start", "t_done", "h2d_ms", "wait_ms", "chain_ms", "d2h_ms"]),
 }
 
 
@@ -75,6 +75,13 @@ def test_autotune_candidates_are_valid_splits():
     small = autotune.candidates(synth.config1(), 152)
     assert {c.get("tune_units") for c in small[1:]} == {152, 304, 1216}
     assert autotune.shape_key(synth.config1(), "GPU") != autotune.shape_key(synth.config2(), "GPU")
+
+
+def test_span_priorities_favour_short_blocks():
+    from psrdada_cpp_gb300 import loadgen
+    p = loadgen.span_priorities([synth.config1(), synth.config3(), synth.config2()])
+    assert p[synth.config1().name] < 0 and p[synth.config3().name] == 0
+    assert p[synth.config1().name] <= p[synth.config2().name] <= p[synth.config3().name]
 
 
 def test_make_config_carries_tune_and_layout():
