@@ -41,6 +41,11 @@ extern "C" {
 #define GSPEC_INTENDED 0  /* item of the heap holding the sample; per-pol baselines */
 #define GSPEC_REFERENCE 1 /* the reference's literal indexing where it stays in bounds */
 
+/* Arithmetic form of the FFT (gspec_config.form). */
+#define GSPEC_FORM_FP32 0 /* FP32 Stockham FFT on the CUDA cores */
+#define GSPEC_FORM_BF16 1 /* four-step DFT-32 stages on the tensor cores, BF16 hi+lo split, FP32 accumulate */
+#define GSPEC_FORM_FP16 2 /* the same with FP16 hi+lo halves */
+
 /* Flags. */
 #define GSPEC_FLAG_SATURATION_RECORD 1u /* append n_out x {sat G0, sat G1} u64 to each output */
 #define GSPEC_FLAG_NO_HOST_BUFFERS 2u   /* no pinned output buffers: the handle is driven only through
@@ -285,6 +290,11 @@ uint64_t gspec_batch_steps(const gspec_batch* b);
 const char* gspec_batch_last_error(const gspec_batch* b);
 
 /* Test entry points of single stages on device memory. */
+/* Tensor-core DFT-1024 (form GSPEC_FORM_BF16 or GSPEC_FORM_FP16) of
+ * ntransforms (a multiple of 4) contiguous FP32 complex sequences: the
+ * split-precision stage of the four-step form on its own (no reference
+ * counterpart: the reference calls cuFFT). */
+int gspec_tc_dft1024_device(const void* d_in, void* d_out, uint32_t ntransforms, int form, void* cuda_stream);
 /* Unpacker::unpack<nbits> (edd/src/Unpacker.cu:124-140): contiguous packed
  * big-endian samples -> float. */
 int gspec_unpack_device(const void* d_raw, uint32_t nbits, uint64_t nsamples, float* d_out, void* cuda_stream);

@@ -1,0 +1,218 @@
+// Tensor-core (tcgen05) DFT-1024 of the split-precision four-step form.
+//
+// A 1024-point DFT is two 32-point DFT stages with a twiddle between them
+// (n = 32a + b, k = c + 32d):
+//   X[c + 32d] = sum_b W32^(bd) * W1024^(bc) * sum_a x[32a + b] W32^(ac).
+// Each stage is one real GEMM on the 5th-generation tensor cores: the rows
+// are the length-32 sub-sequences of four transforms (4 x 32 = 128 rows, the
+// M of one tcgen05.mma), K = 64 real inputs (re, im interleaved), N = 64 real
+// outputs (re, im interleaved), with the constant DFT-32 matrix as B.
+// Precision: operands are split into hi + lo halves in BF16 (or FP16) and
+// the product is accumulated in FP32 in tensor memory as
+//   A_hi B_hi + A_lo B_hi + A_hi B_lo,
+// 12 MMAs of K = 16 per stage; the dropped A_lo B_lo term is ~2^-16 of the
+// result in BF16.
+//
+// Shared-memory operands use the canonical K-major layout without swizzle:
+// 8-row x 16-byte core matrices; element (row, k) of a bf16 matrix sits at
+//   (row / 8) * SBO + (k / 8) * LBO + (row % 8) * 16 + (k % 8) * 2.
+// LBO = 144 bytes (not a multiple of 128) keeps the column-wise operand
+// stores of the second stage free of bank conflicts.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cstdint>
+
+#include "gspec_device.cuh"
+
+namespace gspec {
+namespace tc {
+
+constexpr uint32_t kLBO = 144;
+constexpr uint32_t kSBO = 8 * kLBO;              // 8 K-chunks of 8 elements per row group
+constexpr uint32_t kABytes = 16 * kSBO;          // 128 rows x 64 bf16
+constexpr uint32_t kBBytes = 8 * kSBO;           // 64 rows x 64 bf16
+constexpr uint32_t kTmemCols = 64;               // 128 lanes x 64 fp32 accumulators
+constexpr uint32_t kWaitLimit = 1u << 22;
+
+__host__ __device__ constexpr uint32_t kmaj_off(uint32_t row, uint32_t k) {
+  return (row >> 3) * kSBO + (k >> 3) * kLBO + (row & 7) * 16 + (k & 7) * 2;
+}
+
+// Shared-memory matrix descriptor: start address, leading (K) and stride
+// (row-group) byte offsets, fixed version bits 46-48 = 0b001, no swizzle.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+  return static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4) | (static_cast<uint64_t>(kLBO >> 4) << 16) |
+         (static_cast<uint64_t>(kSBO >> 4) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: D = F32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9, 10-12 = 1) or FP16 (0), both K-major (bits 15, 16 = 0),
+// N >> 3 in bits 17-22, M >> 4 in bits 24-28.
+__host__ __device__ constexpr uint32_t idesc(int M, int N, bool bf16) {
+  return (1u << 4) | ((bf16 ? 1u : 0u) << 7) | ((bf16 ? 1u : 0u) << 10) | (static_cast<uint32_t>(N >> 3) << 17) |
+         (static_cast<uint32_t>(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(dst)), "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t id, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(id), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
+               : "memory");
+}
+
+// 32 consecutive fp32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// hi/lo split of a complex value into two packed 16-bit pairs (re in the low half).
+template <bool BF16>
+__device__ __forceinline__ void split2(float2 v, uint32_t& hi, uint32_t& lo) {
+  if constexpr (BF16) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(v.x, v.y);
+    const float2 hf = __bfloat1622float2(h);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(v.x - hf.x, v.y - hf.y);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
+  } else {
+    const __half2 h = __floats2half2_rn(v.x, v.y);
+    const float2 hf = __half22float2(h);
+    const __half2 l = __floats2half2_rn(v.x - hf.x, v.y - hf.y);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
+  }
+}
+
+// Shared memory of one tile engine (offsets from a 1024-byte aligned base).
+struct TileSmem {
+  char* a_hi;        // kABytes
+  char* a_lo;        // kABytes
+  char* b_hi;        // kBBytes (DFT-32 matrix)
+  char* b_lo;        // kBBytes
+  const float2* w;   // 1024 twiddles W1024^j
+  uint64_t* bar;     // MMA completion barrier
+  uint32_t tmem;     // TMEM base (kTmemCols columns)
+};
+
+// Issues one stage: 12 MMAs (hi*hi, lo*hi, hi*lo over K = 64) and a commit.
+template <bool BF16>
+__device__ __forceinline__ void issue_stage(const TileSmem& s) {
+  constexpr uint32_t id = idesc(128, 64, BF16);
+  const uint32_t ah = smem_addr(s.a_hi), al = smem_addr(s.a_lo);
+  const uint32_t bh = smem_addr(s.b_hi), bl = smem_addr(s.b_lo);
+  fence_after();
+#pragma unroll
+  for (uint32_t ks = 0; ks < 4; ++ks) {
+    const uint32_t off = ks * 2 * kLBO;
+    mma(s.tmem, sdesc(ah + off), sdesc(bh + off), id, ks > 0 ? 1u : 0u);
+    mma(s.tmem, sdesc(al + off), sdesc(bh + off), id, 1u);
+    mma(s.tmem, sdesc(ah + off), sdesc(bl + off), id, 1u);
+  }
+  commit(s.bar);
+}
+
+// DFT-1024 of four transforms by the 128 threads of the calling group.
+// x(t, n) returns input n of transform t; y(t, k, v) takes output k.
+// Returns false if a bounded wait on the tensor cores gave up.
+template <bool BF16, class X, class Y>
+__device__ __forceinline__ bool dft1024_tile(const TileSmem& s, uint32_t& phase, int tid, X x, Y y) {
+  const int t = tid >> 5, lane = tid & 31;
+  // stage 1: row tid = (t, b = lane) holds x[32a + b], a = 0..31
+#pragma unroll
+  for (int kc = 0; kc < 8; ++kc) {
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) split2<BF16>(x(t, 32 * (4 * kc + j) + lane), h[j], l[j]);
+    *reinterpret_cast<uint4*>(s.a_hi + kmaj_off(tid, 8 * kc)) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4*>(s.a_lo + kmaj_off(tid, 8 * kc)) = make_uint4(l[0], l[1], l[2], l[3]);
+  }
+  fence_async_smem();
+  __syncthreads();
+  if (tid == 0) issue_stage<BF16>(s);
+  bool ok = mbar_wait(s.bar, phase, kWaitLimit);
+  phase ^= 1u;
+  fence_after();
+  const uint32_t lane_addr = s.tmem + (static_cast<uint32_t>(t * 32) << 16);
+  float v[32];
+  {
+    // outputs c = 0..15 (columns 0..31), twiddled, into the stage-2 rows (t, c)
+    tmem_ld32(lane_addr, v);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      const float2 z = cmul(make_float2(v[2 * c], v[2 * c + 1]), s.w[lane * c]);
+      uint32_t hi, lo;
+      split2<BF16>(z, hi, lo);
+      *reinterpret_cast<uint32_t*>(s.a_hi + kmaj_off(32 * t + c, 2 * lane)) = hi;
+      *reinterpret_cast<uint32_t*>(s.a_lo + kmaj_off(32 * t + c, 2 * lane)) = lo;
+    }
+    tmem_ld32(lane_addr + 32, v);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      const float2 z = cmul(make_float2(v[2 * c], v[2 * c + 1]), s.w[lane * (c + 16)]);
+      uint32_t hi, lo;
+      split2<BF16>(z, hi, lo);
+      *reinterpret_cast<uint32_t*>(s.a_hi + kmaj_off(32 * t + c + 16, 2 * lane)) = hi;
+      *reinterpret_cast<uint32_t*>(s.a_lo + kmaj_off(32 * t + c + 16, 2 * lane)) = lo;
+    }
+  }
+  fence_before();
+  fence_async_smem();
+  __syncthreads();
+  if (tid == 0) issue_stage<BF16>(s);
+  ok = mbar_wait(s.bar, phase, kWaitLimit) && ok;
+  phase ^= 1u;
+  fence_after();
+  // stage 2: row tid = (t, c = lane) holds X[c + 32d], d = 0..31
+  tmem_ld32(lane_addr, v);
+#pragma unroll
+  for (int d = 0; d < 16; ++d) y(t, lane + 32 * d, make_float2(v[2 * d], v[2 * d + 1]));
+  tmem_ld32(lane_addr + 32, v);
+#pragma unroll
+  for (int d = 0; d < 16; ++d) y(t, lane + 32 * (d + 16), make_float2(v[2 * d], v[2 * d + 1]));
+  fence_before();
+  return ok;
+}
+
+// Copies the DFT-32 operand halves (logical [n][k] 64 x 64 16-bit arrays in
+// global memory) into the canonical layout.
+__device__ __forceinline__ void load_dft32_operand(char* b_hi, char* b_lo, const uint16_t* g_hi, const uint16_t* g_lo,
+                                                   int tid, int nthreads) {
+  for (int i = tid; i < 64 * 64; i += nthreads) {
+    const int n = i >> 6, k = i & 63;
+    *reinterpret_cast<uint16_t*>(b_hi + kmaj_off(n, k)) = g_hi[i];
+    *reinterpret_cast<uint16_t*>(b_lo + kmaj_off(n, k)) = g_lo[i];
+  }
+}
+
+}  // namespace tc
+}  // namespace gspec

@@ -29,6 +29,7 @@ POWER, FULL_STOKES = 0, 1
 INTENDED, REFERENCE = 0, 1
 FLAG_SATURATION_RECORD = 1
 FLAG_NO_HOST_BUFFERS = 2
+FORM_FP32, FORM_BF16, FORM_FP16 = 0, 1, 2
 TUNE_KEYS = ("tune_units", "tune_n1", "tune_scratch_mb")
 
 
@@ -104,6 +105,7 @@ def load_library() -> ctypes.CDLL:
     lib.gspec_gate_device.argtypes = [vp, vp, vp, vp]
     lib.gspec_process_block_noalloc.argtypes = [ctypes.POINTER(GspecConfig), vp, vp, vp, vp, ctypes.c_char_p, sz]
     lib.gspec_query.argtypes = [ctypes.POINTER(GspecConfig), ctypes.POINTER(GspecInfo), ctypes.c_char_p, sz]
+    lib.gspec_tc_dft1024_device.argtypes = [vp, vp, u32, ctypes.c_int, vp]
     from . import serving
     serving.declare(lib)
     _LIB = lib
@@ -364,6 +366,16 @@ def process_block_noalloc(config: GspecConfig, d_block: int, d_baselines: int, d
                                                     ctypes.c_void_p(stream), err, len(err))
     if rc != GSPEC_OK:
         raise GspecError(err.value.decode())
+
+
+def tc_dft1024_device(d_in: int, d_out: int, ntransforms: int, form: int = FORM_BF16, stream: int = 0) -> None:
+    """Tensor-core split-precision DFT-1024 of ntransforms (a multiple of 4)
+    contiguous complex64 sequences in device memory (``gspec_tc_dft1024_device``)."""
+    lib = load_library()
+    rc = lib.gspec_tc_dft1024_device(ctypes.c_void_p(d_in), ctypes.c_void_p(d_out), ntransforms, form,
+                                     ctypes.c_void_p(stream))
+    if rc != GSPEC_OK:
+        raise GspecError(f"gspec_tc_dft1024_device returned {rc}")
 
 
 def unpack_device(d_raw: int, nbits: int, nsamples: int, d_out: int, stream: int = 0) -> None:
