@@ -200,6 +200,48 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+TC_FLOPS_PER_DFT1024 = 2 * 12 * 128 * 64 * 16 * 2 / 4     # 2 stages x 12 MMAs (M128 N64 K16) per 4 transforms
+FALLBACK_BF16_TFLOPS = 1900.0
+
+
+def jobs_per_block(spec) -> int:
+    """FFT jobs of one block of a bench workload (no lost heaps): dual pol,
+    one per (frame, gate with data); single pol, one per frame with both gates
+    plus one per two single-gate frames of the same output spectrum."""
+    from psrdada_cpp_gb300 import synth
+    items = synth.diode_items(spec, 0)[0]
+    state = ((items[spec.selected_side_channel::spec.n_side_channels] >> np.uint64(spec.selected_bit)) & np.uint64(1))
+    sph = spec.heap_size * 8 // spec.nbits
+    per_sample = np.repeat(state.astype(np.int8), sph)[:spec.samples_per_pol]
+    frames = per_sample.reshape(-1, spec.fft_length)
+    has1 = frames.max(axis=1) == 1
+    has0 = frames.min(axis=1) == 0
+    if spec.dual_pol:
+        return int(has0.sum() + has1.sum())
+    per_out = max(1, (spec.samples_per_pol // spec.fft_length) // max(1, spec.naccumulate))
+    mixed = (has0 & has1).reshape(-1, per_out) if frames.shape[0] % per_out == 0 else (has0 & has1)[None]
+    single = (has0 ^ has1).reshape(mixed.shape)
+    return int(mixed.sum() + np.ceil(single.sum(axis=1) / 2).sum())
+
+
+def tensor_roofline(spec, info, form, kernels, nprof, G):
+    """Tensor-core work of the split-precision forms: MMA flops per block
+    over the device time of the passes that run on the tensor cores."""
+    if form == G.FORM_FP32 or int(info.fft_path) != 1:
+        return None
+    n1, n2 = int(info.n1), int(info.n2)
+    jobs = jobs_per_block(spec)
+    transforms = jobs * ((n2 if n1 == 1024 else 0) + (n1 if n2 == 1024 else 0))
+    flops = transforms * TC_FLOPS_PER_DFT1024
+    ms = sum(kernels[k][2] for k in ("fourstep_a", "fourstep_b") if k in kernels
+             and ((k == "fourstep_a" and n1 == 1024) or (k == "fourstep_b" and n2 == 1024))) / nprof
+    ach = flops / (ms / 1e3) / 1e12 if ms > 0 else None
+    return {"bound": "tensor", "mma_flops_per_block": flops, "dft1024_per_block": transforms,
+            "tensor_pass_ms_per_block": round(ms, 4), "achieved_tflops": round(ach, 2) if ach else None,
+            "peak_tflops": FALLBACK_BF16_TFLOPS, "peak_source": "fallback dense bf16 (no measured peak file)",
+            "frac": round(ach / FALLBACK_BF16_TFLOPS, 5) if ach else None}
+
+
 def cpu_cores() -> int:
     try:
         return len(os.sched_getaffinity(0))
@@ -254,7 +296,8 @@ def run_gpu(args):
     spec, kind = workload(args.workload)
     samples_per_step = spec.samples_per_pol * spec.npol
     lay = G.DadaBufferLayout(spec.buffer_size, spec.heap_size, spec.n_side_channels)
-    mk = dict(input_type=G.DUAL_POL if spec.dual_pol else G.SINGLE_POL, device=local)
+    form = {"fp32": G.FORM_FP32, "bf16": G.FORM_BF16, "fp16": G.FORM_FP16}[args.form]
+    mk = dict(input_type=G.DUAL_POL if spec.dual_pol else G.SINGLE_POL, device=local, form=form)
     gs = G.GatedSpectrometer(lay, 0, 0, spec.fft_length, spec.naccumulate, spec.nbits, 100.0, 100.0,
                              G.NullSink(), **mk)
     info = gs.info()
@@ -333,7 +376,7 @@ def run_gpu(args):
     roofline = {
         "bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
         "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} copy bandwidth",
-        "traffic": ncu_traffic(dom, spec.name),
+        "traffic": ncu_traffic(dom, spec.name if args.form == "fp32" else f"{spec.name}_{args.form}"),
         "algorithmic_bytes_per_launch": int(alg_bytes_launch), "mean_launch_ms": round(per_launch_ms, 4),
         "chain": {"ms_per_block": round(chain_ms, 4), "algorithmic_bytes_per_block": in_bytes + out_bytes,
                   "achieved_GBs": round(chain_gbs, 1), "frac": round(chain_gbs / peak, 4)},
@@ -342,6 +385,7 @@ def run_gpu(args):
                     for k, v in kernels.items()},
         "fp32_fft": {"nominal_flops_per_block": fft_flops,
                      "achieved_tflops": round(fft_flops / (chain_ms / 1e3) / 1e12, 2)},
+        "tensor": tensor_roofline(spec, info, form, kernels, nprof, G),
     }
 
     # ---- end to end through the handler API, pinned host blocks
@@ -390,10 +434,12 @@ def run_gpu(args):
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": {"fp32": "f32", "bf16": "bf16 hi+lo, f32 accumulate", "fp16": "f16 hi+lo, f32 accumulate"}[args.form],
+            "data": "synthetic",
             "config": {"workload": spec.name, "fft_length": spec.fft_length, "naccumulate": spec.naccumulate,
                        "nbits": spec.nbits, "pols": spec.npol, "samples_per_pol_per_block": spec.samples_per_pol,
-                       "block_bytes": spec.buffer_size, "form": "fp32",
+                       "block_bytes": spec.buffer_size, "form": args.form,
                        "l2": "inputs larger than L2: %d device blocks of %d B rotate (L2 %d B)" % (nrot, spec.buffer_size, l2_bytes),
                        "parallelism": f"replicas x{ws} (one independent stream per GPU)"},
             "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "roofline": roofline,
@@ -650,6 +696,8 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=["c1", "c2", "c3", "c4", "c5"], default="c2",
                     help="c1-c3 one stream; c4 16 uneven streams in one CUDA graph; c5 the serving loop")
+    ap.add_argument("--form", choices=["fp32", "bf16", "fp16"], default="fp32",
+                    help="FFT arithmetic: FP32 CUDA cores, or tensor-core DFT-32 stages with BF16/FP16 hi+lo halves")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)

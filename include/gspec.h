@@ -80,6 +80,11 @@ typedef struct gspec_config {
    * clamped to the device's range): a server gives latency-critical streams
    * (short blocks) precedence over long blocks of other streams. */
   int32_t stream_priority;
+  /* GSPEC_FORM_FP32 (default) or a tensor-core split-precision form
+   * (GSPEC_FORM_BF16 / GSPEC_FORM_FP16) for fft_length 2^16..2^20: the
+   * four-step passes whose length is 1024 run as two DFT-32 GEMM stages on
+   * the tensor cores (fft_length >= 2^17: N1 = 1024; 2^16: N2 = 1024). */
+  uint32_t form;
 } gspec_config;
 
 typedef struct gspec_info {

@@ -18,6 +18,7 @@
 #include "gspec_kernels.cuh"
 
 #include "gspec_engine_internal.cuh"
+#include "gspec_tc_kernels.cuh"
 
 using namespace gspec;
 
@@ -76,6 +77,16 @@ bool configure(gspec_handle* h) {
     h->path = 1;
     h->N1 = fourstep_n1(static_cast<int>(N));
     h->N2 = fourstep_n2(static_cast<int>(N));
+    if (c.form != GSPEC_FORM_FP32) {
+      // the tensor-core passes are 1024 points long
+      if (N >= (1u << 17)) {
+        h->N1 = 1024;
+        h->N2 = static_cast<uint32_t>(N / 1024);
+      } else if (N == (1u << 16)) {
+        h->N1 = 64;
+        h->N2 = 1024;
+      }
+    }
     if (c.tune_n1) {
       const uint64_t n1 = c.tune_n1;
       if ((n1 & (n1 - 1)) || n1 < 64 || n1 > 1024 || N % n1 || N / n1 < 128 || N / n1 > 1024)
@@ -86,6 +97,9 @@ bool configure(gspec_handle* h) {
   } else {
     return fail("fft_length must be in [32, 2^20]");
   }
+  if (c.form > GSPEC_FORM_FP16) return fail("unknown arithmetic form");
+  if (c.form != GSPEC_FORM_FP32 && (h->path != 1 || (h->N1 != 1024 && h->N2 != 1024)))
+    return fail("the tensor-core forms need fft_length 2^16..2^20 with a 1024-point four-step pass");
   h->dual = c.input_type == GSPEC_DUAL_POL;
   h->npol = h->dual ? 2 : 1;
   const uint64_t scs = c.n_side_channels * 8;
@@ -250,6 +264,10 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
     f.N1 = h->N1;
     f.N2 = h->N2;
     f.maxjobs = h->maxjobs;
+    f.form = h->cfg.form;
+    f.tc_hi = h->d_tc_hi;
+    f.tc_lo = h->d_tc_lo;
+    f.tc_w = h->d_tc_w;
     f.jobs = h->d_jobs;
     f.njobs = h->d_njobs;
     f.dc = h->d_dc;
@@ -300,7 +318,7 @@ void release(gspec_handle* h) {
   }
   void* ptrs[] = {h->d_sat_dev, h->d_baselines, h->d_pol_stats, h->d_tw,   h->d_tw1,   h->d_tw2,  h->d_twA,
                   h->d_twB,     h->d_partial,   h->d_scratch,   h->d_masks, h->d_flags, h->d_jobs, h->d_njobs,
-                  h->d_dc,      h->d_err};
+                  h->d_dc,      h->d_err,       h->d_tc_hi,     h->d_tc_lo, h->d_tc_w};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->h_err) cudaFreeHost(h->h_err);
@@ -456,6 +474,7 @@ uint64_t footprint(const gspec_handle* h) {
     t += sz(static_cast<uint64_t>(h->kchunk) * h->maxjobs * N * sizeof(float2));
     t += sz(h->n_out * h->maxjobs * sizeof(uint32_t)) + sz(h->n_out * sizeof(uint32_t)) +
          sz(2ull * h->n_out * sizeof(uint32_t));
+    if (h->cfg.form != GSPEC_FORM_FP32) t += 2 * sz(4096 * sizeof(uint16_t)) + sz(1024 * sizeof(float2));
   }
   return t;
 }
@@ -573,6 +592,15 @@ gspec_handle* gspec_create(const gspec_config* cfg, char* err, size_t err_len) {
         !dalloc(h, &h->d_njobs, h->n_out * sizeof(uint32_t), "job counts") ||
         !dalloc(h, &h->d_dc, 2ull * h->n_out * sizeof(uint32_t), "dc counts"))
       return bail("");
+    if (cfg->form != GSPEC_FORM_FP32) {
+      if (!dalloc(h, &h->d_tc_hi, 4096 * sizeof(uint16_t), "tensor-core operand") ||
+          !dalloc(h, &h->d_tc_lo, 4096 * sizeof(uint16_t), "tensor-core operand") ||
+          !dalloc(h, &h->d_tc_w, 1024 * sizeof(float2), "tensor-core twiddles"))
+        return bail("");
+      if (!cuda_ok(h, tc::launch_tables(h->d_tc_hi, h->d_tc_lo, h->d_tc_w, cfg->form == GSPEC_FORM_BF16, h->proc),
+                   "tensor-core tables"))
+        return bail("");
+    }
   }
   if (!cuda_ok(h, cudaStreamSynchronize(h->proc), "setup")) return bail("");
   return h;

@@ -48,6 +48,9 @@ struct gspec_handle {
   uint32_t* d_jobs = nullptr;      // four-step job lists [kchunk][maxjobs]
   uint32_t* d_njobs = nullptr;
   uint32_t* d_dc = nullptr;
+  uint16_t* d_tc_hi = nullptr;     // tensor-core form: DFT-32 operand halves
+  uint16_t* d_tc_lo = nullptr;
+  float2* d_tc_w = nullptr;        // W1024 twiddles
   uint32_t maxjobs = 0;
   int32_t heap_shift = -1;
   uint32_t* d_err = nullptr;       // set by kernels whose bounded waits gave up

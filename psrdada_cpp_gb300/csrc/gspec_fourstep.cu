@@ -12,68 +12,12 @@
 // The plan kernel builds each output spectrum's job list (build_jobs): only
 // gates holding data are transformed; gates without data add their constant
 // baseline to bin 0.
+#include "gspec_fourstep_common.cuh"
 #include "gspec_kernels.cuh"
+#include "gspec_tc_kernels.cuh"
 
 namespace gspec {
 
-namespace {
-
-__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// Same commit rule as the shared-memory path: per-pol n0, n1, s0, s1 to
-// pol_stats; n0, n1 summed over pols to the output record; saturation to sat[k].
-template <int NPOL>
-__device__ void commit(const ChainParams& p, const GateStats (&st)[NPOL], uint32_t k, int vals_c,
-                       unsigned long long* red) {
-  constexpr int NV = 4 * NPOL + 4;
-  unsigned long long v[NV];
-  unsigned long long n0 = 0, n1 = 0, s0 = 0, s1 = 0;
-#pragma unroll
-  for (int q = 0; q < NPOL; ++q) {
-    v[4 * q + 0] = st[q].n0;
-    v[4 * q + 1] = st[q].n1;
-    v[4 * q + 2] = static_cast<unsigned long long>(st[q].s0);
-    v[4 * q + 3] = static_cast<unsigned long long>(st[q].s1);
-    n0 += st[q].n0;
-    n1 += st[q].n1;
-    s0 += st[q].sat0;
-    s1 += st[q].sat1;
-  }
-  v[4 * NPOL + 0] = n0;
-  v[4 * NPOL + 1] = n1;
-  v[4 * NPOL + 2] = s0;
-  v[4 * NPOL + 3] = s1;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-  for (int i = 0; i < NV; ++i) {
-    unsigned long long s = warp_sum(v[i]);
-    if (lane == 0) red[warp * NV + i] = s;
-  }
-  __syncthreads();
-  if (threadIdx.x < NV) {
-    unsigned long long tot = 0;
-    for (int w = 0; w < nw; ++w) tot += red[w * NV + threadIdx.x];
-    const int i = threadIdx.x;
-    if (tot) {
-      if (i < 4 * NPOL) {
-        atomicAdd(p.pol_stats + i, tot);
-      } else if (i - 4 * NPOL < 2) {
-        unsigned long long* cnt =
-            reinterpret_cast<unsigned long long*>(p.out + k * p.out_rec + static_cast<uint64_t>(vals_c) * 4);
-        atomicAdd(cnt + (i - 4 * NPOL), tot);
-      } else {
-        atomicAdd(p.sat + 2 * k + (i - 4 * NPOL - 2), tot);
-      }
-    }
-  }
-  __syncthreads();
-}
-
-}  // namespace
 
 // One thread per output spectrum of the launch: its job list.
 __global__ void fourstep_plan_kernel(FourStepParams p, int dual) {
@@ -191,7 +135,7 @@ __global__ void __launch_bounds__(PassACfg<N1>::THREADS) fourstep_a_kernel(FourS
       dst[static_cast<size_t>(k1) * N2 + n2] = cmul(v, W);
     }
   }
-  commit<NPOL>(p.c, st, k, (DUAL ? 8 : 2) * static_cast<int>(N / 2 + 1), red);
+  commit_stats<NPOL>(p.c, st, k, (DUAL ? 8 : 2) * static_cast<int>(N / 2 + 1), red);
 }
 
 #ifndef GSPEC_PASSB_THREADS
@@ -215,22 +159,6 @@ struct PassBCfg {
   static constexpr size_t SMEM = 2 * STAGE_BYTES + WORK_BYTES + TW_BYTES + JW_BYTES + 2 * sizeof(uint64_t);
 };
 
-// Row pair rp holds rows rp and N1-rp (rp = 0: rows 0 and N1/2).  Accumulator
-// slot a of the pair maps to these bins:
-//   rp != 0: a < N2/2 -> row rp, k2 = a (mirror: row N1-rp, N2-1-a);
-//            a >= N2/2 -> row N1-rp, k2 = a - N2/2 (mirror: row rp, N2-1-k2)
-//   rp == 0: a <= N2/2 -> row 0, k2 = a (mirror: row 0, N2-a mod N2);
-//            a > N2/2 -> row N1/2, k2 = a-N2/2-1 (mirror: row N1/2, N2-1-k2)
-template <int N2>
-__device__ __forceinline__ void pair_slot(uint32_t rp, int a, int& r, int& k2, int& pr, int& k2p) {
-  if (rp != 0) {
-    if (a < N2 / 2) { r = 0; k2 = a; pr = 1; k2p = N2 - 1 - a; }
-    else { r = 1; k2 = a - N2 / 2; pr = 0; k2p = N2 - 1 - k2; }
-  } else {
-    if (a <= N2 / 2) { r = 0; k2 = a; pr = 0; k2p = (N2 - a) & (N2 - 1); }
-    else { r = 1; k2 = a - N2 / 2 - 1; pr = 1; k2p = N2 - 1 - k2; }
-  }
-}
 
 // grid.x = nk * N1/2: unit (output spectrum k, row pair rp).  J jobs are
 // transformed together (2*T2 threads each).  Their rows arrive by TMA bulk
@@ -472,6 +400,8 @@ cudaError_t launch_fourstep(int N, int nbits, bool dual, const FourStepParams& p
     fourstep_plan_kernel<<<(p.nk + 63) / 64, 64, 0, s>>>(p, dual ? 1 : 0);
     return cudaGetLastError();
   }
+  if (p.form != 0 && ((pass == 0 && p.N1 == 1024) || (pass == 1 && p.N2 == 1024)))
+    return tc::launch_tc_pass(pass, nbits, dual, p, s);
   return dual ? launch_fs<true>(nbits, p, pass, s) : launch_fs<false>(nbits, p, pass, s);
 }
 

@@ -1,0 +1,82 @@
+// Pieces shared by the FP32 four-step passes (gspec_fourstep.cu) and the
+// tensor-core passes (gspec_tc.cu).
+#pragma once
+
+#include "gspec_kernels.cuh"
+
+namespace gspec {
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Same commit rule as the shared-memory path: per-pol n0, n1, s0, s1 to
+// pol_stats; n0, n1 summed over pols to the output record; saturation to sat[k].
+template <int NPOL>
+__device__ void commit_stats(const ChainParams& p, const GateStats (&st)[NPOL], uint32_t k, int vals_c,
+                       unsigned long long* red) {
+  constexpr int NV = 4 * NPOL + 4;
+  unsigned long long v[NV];
+  unsigned long long n0 = 0, n1 = 0, s0 = 0, s1 = 0;
+#pragma unroll
+  for (int q = 0; q < NPOL; ++q) {
+    v[4 * q + 0] = st[q].n0;
+    v[4 * q + 1] = st[q].n1;
+    v[4 * q + 2] = static_cast<unsigned long long>(st[q].s0);
+    v[4 * q + 3] = static_cast<unsigned long long>(st[q].s1);
+    n0 += st[q].n0;
+    n1 += st[q].n1;
+    s0 += st[q].sat0;
+    s1 += st[q].sat1;
+  }
+  v[4 * NPOL + 0] = n0;
+  v[4 * NPOL + 1] = n1;
+  v[4 * NPOL + 2] = s0;
+  v[4 * NPOL + 3] = s1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    unsigned long long s = warp_sum_u64(v[i]);
+    if (lane == 0) red[warp * NV + i] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    unsigned long long tot = 0;
+    for (int w = 0; w < nw; ++w) tot += red[w * NV + threadIdx.x];
+    const int i = threadIdx.x;
+    if (tot) {
+      if (i < 4 * NPOL) {
+        atomicAdd(p.pol_stats + i, tot);
+      } else if (i - 4 * NPOL < 2) {
+        unsigned long long* cnt =
+            reinterpret_cast<unsigned long long*>(p.out + k * p.out_rec + static_cast<uint64_t>(vals_c) * 4);
+        atomicAdd(cnt + (i - 4 * NPOL), tot);
+      } else {
+        atomicAdd(p.sat + 2 * k + (i - 4 * NPOL - 2), tot);
+      }
+    }
+  }
+  __syncthreads();
+}
+
+
+// Row pair rp holds rows rp and N1-rp (rp = 0: rows 0 and N1/2).  Accumulator
+// slot a of the pair maps to these bins:
+//   rp != 0: a < N2/2 -> row rp, k2 = a (mirror: row N1-rp, N2-1-a);
+//            a >= N2/2 -> row N1-rp, k2 = a - N2/2 (mirror: row rp, N2-1-k2)
+//   rp == 0: a <= N2/2 -> row 0, k2 = a (mirror: row 0, N2-a mod N2);
+//            a > N2/2 -> row N1/2, k2 = a-N2/2-1 (mirror: row N1/2, N2-1-k2)
+template <int N2>
+__device__ __forceinline__ void pair_slot(uint32_t rp, int a, int& r, int& k2, int& pr, int& k2p) {
+  if (rp != 0) {
+    if (a < N2 / 2) { r = 0; k2 = a; pr = 1; k2p = N2 - 1 - a; }
+    else { r = 1; k2 = a - N2 / 2; pr = 0; k2p = N2 - 1 - k2; }
+  } else {
+    if (a <= N2 / 2) { r = 0; k2 = a; pr = 0; k2p = (N2 - a) & (N2 - 1); }
+    else { r = 1; k2 = a - N2 / 2 - 1; pr = 1; k2p = N2 - 1 - k2; }
+  }
+}
+
+}  // namespace gspec

@@ -45,6 +45,11 @@ struct FourStepParams {
   uint32_t* jobs;                  // [n_out][maxjobs] job list per output spectrum
   uint32_t* njobs;                 // [n_out]
   uint32_t* dc;                    // [n_out][2] frames without data per gate
+  // tensor-core form (form != 0): DFT-32 operand halves and W1024 twiddles
+  uint32_t form;                   // GSPEC_FORM_*
+  const uint16_t* tc_hi;
+  const uint16_t* tc_lo;
+  const float2* tc_w;
 };
 
 // Host-side launchers (gspec_kernels.cu).

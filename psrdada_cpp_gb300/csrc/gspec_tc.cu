@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(128) dft1024_test_kernel(const float2* __restr
   uint32_t phase = 0;
   const bool ok = dft1024_tile<BF16>(
       s, phase, tid, [&](int t, int n) { return xs[t * 1024 + n]; },
-      [&](int t, int k, float2 v) { out[(static_cast<size_t>(blockIdx.x) * 4 + t) * 1024 + k] = v; });
+      [&](int t, int k, float2 v) { out[(static_cast<size_t>(blockIdx.x) * 4 + t) * 1024 + k] = v; }, [] {});
   if (!ok && err) atomicExch(err, 3u);
   __syncthreads();
   fence_after();
@@ -132,3 +132,371 @@ extern "C" int gspec_tc_dft1024_device(const void* d_in, void* d_out, uint32_t n
   cudaFree(err);
   return rc;
 }
+
+// ====================================================================
+// Four-step passes of the tensor-core form (N1 = 1024 for pass A, N2 = 1024
+// for pass B).  They follow the FP32 passes of gspec_fourstep.cu step by
+// step; only the 1024-point FFT of each column / row is replaced by
+// dft1024_tile on the tensor cores.
+// ====================================================================
+#include "gspec_fourstep_common.cuh"
+
+namespace gspec {
+namespace tc {
+
+constexpr int kPassThreads = 128;
+constexpr int kColStride = spad_size(1024) + 1;   // odd: column-wise reads are conflict-free
+constexpr int kRowStride = spad_size(1024);
+
+// FP16 operand scales (powers of two): pass A inputs are at most 2^11 in
+// magnitude, its stage-1 outputs at most 2^11 * 32 * sqrt(2); pass B inputs
+// (pass A outputs) at most 2^11 * 1024 * sqrt(2).
+template <bool BF16> struct Scales {
+  static constexpr float a1 = 1.f, a2 = BF16 ? 1.f : 0.25f;
+  static constexpr float b1 = BF16 ? 1.f : 1.f / 64, b2 = BF16 ? 1.f : 1.f / 32;
+};
+
+struct PassALayout {
+  static constexpr size_t A = 0;
+  static constexpr size_t B = 2 * kABytes;
+  static constexpr size_t S = B + 2 * kBBytes;
+  static constexpr size_t W = S + static_cast<size_t>(4) * kColStride * sizeof(float2);
+  static constexpr size_t RED = W + 1024 * sizeof(float2);
+  static constexpr size_t BAR = RED + (kPassThreads / 32) * 12 * 8;
+  static constexpr size_t BYTES = BAR + 16;
+};
+
+// grid.x = nk * maxjobs * (N2 / 4): (output spectrum, job, tile of 4 columns)
+template <int NBITS, bool DUAL, bool BF16>
+__global__ void __launch_bounds__(kPassThreads, 2) tc_a_kernel(FourStepParams p) {
+  constexpr int N1 = 1024, BC = 4;
+  constexpr int G = Group<NBITS>::samples;
+  constexpr int NPOL = DUAL ? 2 : 1;
+  extern __shared__ __align__(1024) char smem[];
+  using L = PassALayout;
+  TileSmem s;
+  s.a_hi = smem + L::A;
+  s.a_lo = smem + L::A + kABytes;
+  s.b_hi = smem + L::B;
+  s.b_lo = smem + L::B + kBBytes;
+  float2* S = reinterpret_cast<float2*>(smem + L::S);
+  float2* w = reinterpret_cast<float2*>(smem + L::W);
+  unsigned long long* red = reinterpret_cast<unsigned long long*>(smem + L::RED);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L::BAR);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
+  s.w = w;
+  s.bar = bar;
+
+  const uint32_t N2 = p.N2;
+  const uint32_t N = N1 * N2;
+  const uint32_t tiles = N2 / BC;
+  const uint32_t tile = blockIdx.x % tiles;
+  const uint32_t j = (blockIdx.x / tiles) % p.maxjobs;
+  const uint32_t kk = blockIdx.x / (tiles * p.maxjobs);
+  const uint32_t k = p.k0 + kk;
+  if (j >= p.njobs[k]) return;
+  const uint32_t job = p.jobs[k * p.maxjobs + j];
+  const uint32_t fa = job_fa(job), ga = job_ga(job), fb = job_fb(job), gb = job_gb(job);
+  const uint32_t frA = k * p.c.nacc + fa;
+  const uint32_t frB = k * p.c.nacc + fb;
+  const uint32_t c0 = tile * BC;
+  const int tid = threadIdx.x;
+
+  float bl[2 * NPOL];
+#pragma unroll
+  for (int i = 0; i < 2 * NPOL; ++i) bl[i] = p.c.baselines[i];
+  load_dft32_operand(s.b_hi, s.b_lo, p.tc_hi, p.tc_lo, tid, kPassThreads);
+  for (int i = tid; i < 1024; i += kPassThreads) w[i] = p.tc_w[i];
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (tid < 32) tmem_alloc(tmem_slot, kTmemCols);
+
+  // unpack + gate this tile's 4 columns of all N1 rows (one group per row)
+  const uint32_t gbase = (c0 / G) * G;
+  const int keep0 = static_cast<int>(c0 - gbase);
+  const bool count_stats = c0 == gbase;
+  const uint32_t sg_a = count_stats ? (DUAL ? (1u << ga) : 3u) : 0u;
+  GateStats st[NPOL];
+  for (int n1 = tid; n1 < N1; n1 += kPassThreads) {
+    const uint32_t off = N2 * n1 + gbase;
+    float re[G], im[G];
+    if constexpr (DUAL) {
+      gate_group1<NBITS>(p.c.g, 0, frA * N + off, bl[ga], ga, re, st[0], count_stats);
+      gate_group1<NBITS>(p.c.g, 1, frA * N + off, bl[2 + ga], ga, im, st[NPOL - 1], count_stats);
+    } else if (fb == fa) {
+      gate_group<NBITS>(p.c.g, 0, frA * N + off, bl[0], bl[1], re, im, st[0], sg_a);
+    } else {
+      gate_group1<NBITS>(p.c.g, 0, frA * N + off, bl[ga], ga, re, st[0], count_stats);
+      if (fb != kNoFrame) {
+        gate_group1<NBITS>(p.c.g, 0, frB * N + off, bl[gb], gb, im, st[0], count_stats);
+      } else {
+#pragma unroll
+        for (int e = 0; e < G; ++e) im[e] = 0.f;
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < G; ++e)
+      if (e >= keep0 && e < keep0 + BC) S[(e - keep0) * kColStride + spad(n1)] = make_float2(re[e], im[e]);
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  s.tmem = *tmem_slot;
+  uint32_t phase = 0;
+  const bool ok = dft1024_tile<BF16>(
+      s, phase, tid, [&](int t, int n) { return S[t * kColStride + spad(n)]; },
+      [&](int t, int k1, float2 v) { S[t * kColStride + spad(k1)] = v; }, [] {}, Scales<BF16>::a1,
+      Scales<BF16>::a2);
+  if (!ok && tid == 0 && p.c.dev_err) atomicExch(p.c.dev_err, 3u);
+  __syncthreads();
+  // twiddle W_N^(n2*k1) and store Y[k1][n2] (as the FP32 pass)
+  float2* dst = p.scratch + (static_cast<size_t>(kk) * p.maxjobs + j) * N;
+  {
+    constexpr int KS = kPassThreads / BC;
+    constexpr int PPT = N1 / KS;
+    const int col = tid % BC;
+    const uint32_t n2 = c0 + col;
+    auto exact = [&](uint32_t m) { return cmul(__ldg(&p.twA[m >> 10]), __ldg(&p.twB[m & 1023])); };
+    const float2 D = exact(n2 * KS);
+    float2 W = make_float2(1.f, 0.f);
+#pragma unroll 4
+    for (int i = 0; i < PPT; ++i) {
+      const int k1 = tid / BC + KS * i;
+      W = (i & 3) == 0 ? exact(n2 * static_cast<uint32_t>(k1)) : cmul(W, D);
+      dst[static_cast<size_t>(k1) * N2 + n2] = cmul(S[col * kColStride + spad(k1)], W);
+    }
+  }
+  commit_stats<NPOL>(p.c, st, k, (DUAL ? 8 : 2) * static_cast<int>(N / 2 + 1), red);
+  fence_after();
+  if (tid < 32) tmem_dealloc(s.tmem, kTmemCols);
+}
+
+template <bool DUAL>
+struct PassBLayout {
+  static constexpr int J = 2;                        // jobs per group: 2 jobs x 2 rows = one tile
+  static constexpr int VALS = DUAL ? 8 : 2;
+  static constexpr int BPT = (1024 + 1 + kPassThreads - 1) / kPassThreads;
+  static constexpr size_t A = 0;                     // operands; the transformed rows ("work") alias them
+  static constexpr size_t B = 2 * kABytes;
+  static constexpr size_t STAGE = B + 2 * kBBytes;
+  static constexpr size_t W = STAGE + static_cast<size_t>(J) * 2 * 1024 * sizeof(float2);
+  static constexpr size_t JW = W + 1024 * sizeof(float2);
+  static constexpr size_t BAR = JW + 16;
+  static constexpr size_t BYTES = BAR + 32;
+  static_assert(static_cast<size_t>(4) * kRowStride * sizeof(float2) <= 2 * kABytes, "work fits the operands");
+};
+
+// grid.x = nk * N1/2: unit (output spectrum k, row pair rp); jobs two at a
+// time: their rows arrive by one TMA bulk-copy stage, which is refilled for
+// the next group as soon as the first DFT stage has read it.
+template <bool DUAL, bool BF16>
+__global__ void __launch_bounds__(kPassThreads, 2) tc_b_kernel(FourStepParams p) {
+  constexpr int N2 = 1024;
+  using L = PassBLayout<DUAL>;
+  constexpr int J = L::J, BPT = L::BPT, VALS = L::VALS;
+  constexpr uint32_t kRowBytes = N2 * sizeof(float2);
+  extern __shared__ __align__(1024) char smem[];
+  TileSmem s;
+  s.a_hi = smem + L::A;
+  s.a_lo = smem + L::A + kABytes;
+  s.b_hi = smem + L::B;
+  s.b_lo = smem + L::B + kBBytes;
+  float2* work = reinterpret_cast<float2*>(smem + L::A);
+  float2* stage = reinterpret_cast<float2*>(smem + L::STAGE);
+  float2* w = reinterpret_cast<float2*>(smem + L::W);
+  uint32_t* jw = reinterpret_cast<uint32_t*>(smem + L::JW);
+  uint64_t* tma_bar = reinterpret_cast<uint64_t*>(smem + L::BAR);
+  uint64_t* mma_bar = tma_bar + 1;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tma_bar + 2);
+  s.w = w;
+  s.bar = mma_bar;
+
+  const uint32_t N1 = p.N1;
+  const uint32_t N = N1 * N2;
+  const uint32_t C = N / 2 + 1;
+  const uint32_t half = N1 / 2;
+  const uint32_t kk = blockIdx.x / half;
+  const uint32_t k = p.k0 + kk;
+  const uint32_t rp = blockIdx.x % half;
+  const uint32_t rowA = rp, rowB = rp == 0 ? half : N1 - rp;
+  const int nbins = rp == 0 ? N2 + 1 : N2;
+  const int tid = threadIdx.x;
+  const uint32_t njobs = p.njobs[k];
+  const uint32_t* jobs = p.jobs + k * p.maxjobs;
+  const uint32_t ngroups = (njobs + J - 1) / J;
+
+  if (tid == 0) {
+    mbar_init(tma_bar, 1);
+    mbar_init(mma_bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (tid < 32) tmem_alloc(tmem_slot, kTmemCols);
+  load_dft32_operand(s.b_hi, s.b_lo, p.tc_hi, p.tc_lo, tid, kPassThreads);
+  for (int i = tid; i < 1024; i += kPassThreads) w[i] = p.tc_w[i];
+  fence_before();
+  __syncthreads();
+  fence_after();
+  s.tmem = *tmem_slot;
+
+  // thread 0: rows of job group g into the stage
+  auto issue = [&](uint32_t g) {
+    const uint32_t nq = min(static_cast<uint32_t>(J), njobs - g * J);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(tma_bar, nq * 2 * kRowBytes);
+    for (uint32_t qq = 0; qq < nq; ++qq) {
+      const float2* seq = p.scratch + (static_cast<size_t>(kk) * p.maxjobs + g * J + qq) * N;
+      float2* dst = stage + qq * 2 * N2;
+      bulk_g2s(dst, seq + static_cast<size_t>(rowA) * N2, kRowBytes, tma_bar);
+      bulk_g2s(dst + N2, seq + static_cast<size_t>(rowB) * N2, kRowBytes, tma_bar);
+    }
+  };
+  if (tid == 0 && ngroups > 0) issue(0);
+
+  float acc[BPT][VALS];
+#pragma unroll
+  for (int i = 0; i < BPT; ++i)
+#pragma unroll
+    for (int v = 0; v < VALS; ++v) acc[i][v] = 0.f;
+
+  uint32_t phase = 0;
+  bool mma_ok = true;
+  for (uint32_t g = 0; g < ngroups; ++g) {
+    const bool ok = mbar_wait(tma_bar, g & 1u, 1u << 24);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        if (p.c.dev_err) atomicExch(p.c.dev_err, 2u);
+        mbar_wait(tma_bar, g & 1u, 1u << 20);   // a bounded chance for the copies in flight to land
+      }
+      __syncthreads();
+      break;
+    }
+    const uint32_t j0 = g * J;
+    const int nq = static_cast<int>(min(static_cast<uint32_t>(J), njobs - j0));
+    if (tid < nq) jw[tid] = jobs[j0 + tid];
+    mma_ok = dft1024_tile<BF16>(
+                 s, phase, tid, [&](int t, int n) { return stage[t * N2 + n]; },
+                 [&](int t, int k2, float2 v) { work[t * kRowStride + spad(k2)] = v; },
+                 [&] {
+                   if (tid == 0 && g + 1 < ngroups) issue(g + 1);
+                 },
+                 Scales<BF16>::b1, Scales<BF16>::b2) &&
+             mma_ok;
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < BPT; ++i) {
+      const int a = tid + i * kPassThreads;
+      if (a >= nbins) continue;
+      int r, k2, pr, k2p;
+      pair_slot<N2>(rp, a, r, k2, pr, k2p);
+      for (int qq = 0; qq < nq; ++qq) {
+        const uint32_t job = jw[qq];
+        const float2 za = work[(2 * qq + r) * kRowStride + spad(k2)];
+        const float2 zb = work[(2 * qq + pr) * kRowStride + spad(k2p)];
+        const uint32_t ga = job_ga(job);
+        if constexpr (!DUAL) {
+          const float sx = za.x + zb.x, sy = za.y - zb.y;
+          const float dx = za.x - zb.x, dy = za.y + zb.y;
+          const float pa = 0.25f * fmaf(sx, sx, sy * sy);
+          const float pb = job_fb(job) != kNoFrame ? 0.25f * fmaf(dx, dx, dy * dy) : 0.f;
+          const uint32_t gb = job_gb(job);
+          acc[i][0] += (ga == 0 ? pa : 0.f) + (gb == 0 ? pb : 0.f);
+          acc[i][1] += (ga == 1 ? pa : 0.f) + (gb == 1 ? pb : 0.f);
+        } else {
+          const float p1x = 0.5f * (za.x + zb.x), p1y = 0.5f * (za.y - zb.y);
+          const float p2x = 0.5f * (za.y + zb.y), p2y = -0.5f * (za.x - zb.x);
+          const float a1 = fmaf(p1x, p1x, p1y * p1y);
+          const float a2 = fmaf(p2x, p2x, p2y * p2y);
+          const float I = a1 + a2, Q = a1 - a2;
+          const float U = 2.f * fmaf(p1x, p2x, p1y * p2y);
+          const float V = -2.f * fmaf(p1y, p2x, -p1x * p2y);
+          if (ga == 0) {
+            acc[i][0] += I;
+            acc[i][2] += Q;
+            acc[i][4] += U;
+            acc[i][6] += V;
+          } else {
+            acc[i][1] += I;
+            acc[i][3] += Q;
+            acc[i][5] += U;
+            acc[i][7] += V;
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (!mma_ok && tid == 0 && p.c.dev_err) atomicExch(p.c.dev_err, 3u);
+  // gates without data: constant baseline in bin 0 (row pair 0, slot a = 0)
+  if (rp == 0 && tid == 0) {
+    const float n = static_cast<float>(N);
+    for (int gate = 0; gate < 2; ++gate) {
+      const float cnt = static_cast<float>(p.dc[2 * k + gate]);
+      if (cnt == 0.f) continue;
+      if constexpr (!DUAL) {
+        const float d = n * p.c.baselines[gate];
+        acc[0][gate] += cnt * d * d;
+      } else {
+        const float x = n * p.c.baselines[gate], y = n * p.c.baselines[2 + gate];
+        acc[0][0 + gate] += cnt * (x * x + y * y);
+        acc[0][2 + gate] += cnt * (x * x - y * y);
+        acc[0][4 + gate] += cnt * (2.f * x * y);
+      }
+    }
+  }
+  float* outf = reinterpret_cast<float*>(p.c.out + k * p.c.out_rec);
+#pragma unroll
+  for (int i = 0; i < BPT; ++i) {
+    const int a = tid + i * kPassThreads;
+    if (a >= nbins) continue;
+    uint32_t c;
+    if (rp != 0) {
+      c = a < N2 / 2 ? rp + N1 * a : (N1 - rp) + N1 * (a - N2 / 2);
+    } else {
+      c = a <= N2 / 2 ? N1 * a : half + N1 * (a - N2 / 2 - 1);
+    }
+#pragma unroll
+    for (int v = 0; v < VALS; ++v) outf[static_cast<size_t>(v) * C + c] += acc[i][v];
+  }
+  fence_after();
+  if (tid < 32) tmem_dealloc(s.tmem, kTmemCols);
+}
+
+template <class K>
+static cudaError_t run_tc(K kern, unsigned grid, size_t smem, const FourStepParams& p, cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  kern<<<grid, kPassThreads, smem, s>>>(p);
+  return cudaGetLastError();
+}
+
+template <bool BF16>
+static cudaError_t launch_pass(int pass, int nbits, bool dual, const FourStepParams& p, cudaStream_t s) {
+  if (pass == 0) {
+    if (p.N1 != 1024) return cudaErrorInvalidValue;
+    const unsigned grid = p.nk * p.maxjobs * (p.N2 / 4);
+    const size_t sm = PassALayout::BYTES;
+    switch (nbits * 2 + (dual ? 1 : 0)) {
+      case 16: return run_tc(tc_a_kernel<8, false, BF16>, grid, sm, p, s);
+      case 17: return run_tc(tc_a_kernel<8, true, BF16>, grid, sm, p, s);
+      case 20: return run_tc(tc_a_kernel<10, false, BF16>, grid, sm, p, s);
+      case 21: return run_tc(tc_a_kernel<10, true, BF16>, grid, sm, p, s);
+      case 24: return run_tc(tc_a_kernel<12, false, BF16>, grid, sm, p, s);
+      case 25: return run_tc(tc_a_kernel<12, true, BF16>, grid, sm, p, s);
+    }
+    return cudaErrorInvalidValue;
+  }
+  if (p.N2 != 1024) return cudaErrorInvalidValue;
+  const unsigned grid = p.nk * (p.N1 / 2);
+  return dual ? run_tc(tc_b_kernel<true, BF16>, grid, PassBLayout<true>::BYTES, p, s)
+              : run_tc(tc_b_kernel<false, BF16>, grid, PassBLayout<false>::BYTES, p, s);
+}
+
+cudaError_t launch_tc_pass(int pass, int nbits, bool dual, const FourStepParams& p, cudaStream_t s) {
+  return p.form == GSPEC_FORM_FP16 ? launch_pass<false>(pass, nbits, dual, p, s)
+                                   : launch_pass<true>(pass, nbits, dual, p, s);
+}
+
+}  // namespace tc
+}  // namespace gspec

@@ -141,23 +141,32 @@ __device__ __forceinline__ void issue_stage(const TileSmem& s) {
   commit(s.bar);
 }
 
-// DFT-1024 of four transforms by the 128 threads of the calling group.
+__device__ __forceinline__ float2 scale2(float2 v, float f) { return make_float2(v.x * f, v.y * f); }
+
+// DFT-1024 of four transforms by the 128 threads of the calling group
+// (thread tid of the group; all threads of the block call it together).
 // x(t, n) returns input n of transform t; y(t, k, v) takes output k.
-// Returns false if a bounded wait on the tensor cores gave up.
-template <bool BF16, class X, class Y>
-__device__ __forceinline__ bool dft1024_tile(const TileSmem& s, uint32_t& phase, int tid, X x, Y y) {
+// mid() runs on every thread once the inputs have been read (after the
+// first barrier), e.g. to start loading the next inputs.  sc1 and sc2 scale
+// the operands of the two stages by powers of two (the FP16 form keeps them
+// in range); the outputs are scaled back exactly.  Returns false if a
+// bounded wait on the tensor cores gave up.
+template <bool BF16, class X, class Y, class M>
+__device__ __forceinline__ bool dft1024_tile(const TileSmem& s, uint32_t& phase, int tid, X x, Y y, M mid,
+                                             float sc1 = 1.f, float sc2 = 1.f) {
   const int t = tid >> 5, lane = tid & 31;
   // stage 1: row tid = (t, b = lane) holds x[32a + b], a = 0..31
 #pragma unroll
   for (int kc = 0; kc < 8; ++kc) {
     uint32_t h[4], l[4];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) split2<BF16>(x(t, 32 * (4 * kc + j) + lane), h[j], l[j]);
+    for (int j = 0; j < 4; ++j) split2<BF16>(scale2(x(t, 32 * (4 * kc + j) + lane), sc1), h[j], l[j]);
     *reinterpret_cast<uint4*>(s.a_hi + kmaj_off(tid, 8 * kc)) = make_uint4(h[0], h[1], h[2], h[3]);
     *reinterpret_cast<uint4*>(s.a_lo + kmaj_off(tid, 8 * kc)) = make_uint4(l[0], l[1], l[2], l[3]);
   }
   fence_async_smem();
   __syncthreads();
+  mid();
   if (tid == 0) issue_stage<BF16>(s);
   bool ok = mbar_wait(s.bar, phase, kWaitLimit);
   phase ^= 1u;
@@ -169,7 +178,7 @@ __device__ __forceinline__ bool dft1024_tile(const TileSmem& s, uint32_t& phase,
     tmem_ld32(lane_addr, v);
 #pragma unroll
     for (int c = 0; c < 16; ++c) {
-      const float2 z = cmul(make_float2(v[2 * c], v[2 * c + 1]), s.w[lane * c]);
+      const float2 z = scale2(cmul(make_float2(v[2 * c], v[2 * c + 1]), s.w[lane * c]), sc2);
       uint32_t hi, lo;
       split2<BF16>(z, hi, lo);
       *reinterpret_cast<uint32_t*>(s.a_hi + kmaj_off(32 * t + c, 2 * lane)) = hi;
@@ -178,7 +187,7 @@ __device__ __forceinline__ bool dft1024_tile(const TileSmem& s, uint32_t& phase,
     tmem_ld32(lane_addr + 32, v);
 #pragma unroll
     for (int c = 0; c < 16; ++c) {
-      const float2 z = cmul(make_float2(v[2 * c], v[2 * c + 1]), s.w[lane * (c + 16)]);
+      const float2 z = scale2(cmul(make_float2(v[2 * c], v[2 * c + 1]), s.w[lane * (c + 16)]), sc2);
       uint32_t hi, lo;
       split2<BF16>(z, hi, lo);
       *reinterpret_cast<uint32_t*>(s.a_hi + kmaj_off(32 * t + c + 16, 2 * lane)) = hi;
@@ -193,12 +202,13 @@ __device__ __forceinline__ bool dft1024_tile(const TileSmem& s, uint32_t& phase,
   phase ^= 1u;
   fence_after();
   // stage 2: row tid = (t, c = lane) holds X[c + 32d], d = 0..31
+  const float inv = 1.f / (sc1 * sc2);
   tmem_ld32(lane_addr, v);
 #pragma unroll
-  for (int d = 0; d < 16; ++d) y(t, lane + 32 * d, make_float2(v[2 * d], v[2 * d + 1]));
+  for (int d = 0; d < 16; ++d) y(t, lane + 32 * d, make_float2(v[2 * d] * inv, v[2 * d + 1] * inv));
   tmem_ld32(lane_addr + 32, v);
 #pragma unroll
-  for (int d = 0; d < 16; ++d) y(t, lane + 32 * (d + 16), make_float2(v[2 * d], v[2 * d + 1]));
+  for (int d = 0; d < 16; ++d) y(t, lane + 32 * (d + 16), make_float2(v[2 * d] * inv, v[2 * d + 1] * inv));
   fence_before();
   return ok;
 }

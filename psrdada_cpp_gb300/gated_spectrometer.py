@@ -54,6 +54,7 @@ class GspecConfig(ctypes.Structure):
         ("tune_n1", ctypes.c_uint32),
         ("tune_scratch_mb", ctypes.c_uint32),
         ("stream_priority", ctypes.c_int32),
+        ("form", ctypes.c_uint32),
     ]
 
 
@@ -231,7 +232,7 @@ class GatedSpectrometer:
                  fft_length: int, naccumulate: int, nbits: int, input_level: float,
                  output_level: float, handler, input_type: int = SINGLE_POL,
                  output_type: int | None = None, convention: int = INTENDED, device: int = 0,
-                 flags: int = 0, tune: dict | None = None):
+                 flags: int = 0, tune: dict | None = None, form: int = 0):
         self._lib = load_library()
         if output_type is None:
             output_type = FULL_STOKES if input_type == DUAL_POL else POWER
@@ -240,7 +241,7 @@ class GatedSpectrometer:
             n_side_channels=layout.getNSideChannels(), selected_side_channel=selectedSideChannel,
             selected_bit=selectedBit, fft_length=fft_length, naccumulate=naccumulate, nbits=nbits,
             input_type=input_type, output_type=output_type, convention=convention,
-            input_level=input_level, output_level=output_level, device=device, flags=flags,
+            input_level=input_level, output_level=output_level, device=device, flags=flags, form=form,
             **{k: int(v) for k, v in (tune or {}).items() if k in TUNE_KEYS})
         err = ctypes.create_string_buffer(512)
         h = self._lib.gspec_create(ctypes.byref(cfg), err, len(err))

@@ -75,10 +75,10 @@ def declare(lib) -> None:
 
 
 def make_config(spec, device: int = 0, flags: int = 0, tune: dict | None = None,
-                convention: int = INTENDED, priority: int = 0) -> GspecConfig:
+                convention: int = INTENDED, priority: int = 0, form: int = 0) -> GspecConfig:
     """``GspecConfig`` of a ``synth.StreamSpec`` (selected side channel/bit, layout, shape);
     ``priority`` is the CUDA stream priority (negative = higher)."""
-    return GspecConfig(stream_priority=priority,
+    return GspecConfig(stream_priority=priority, form=form,
         buffer_size=spec.buffer_size, heap_size=spec.heap_size, n_side_channels=spec.n_side_channels,
         selected_side_channel=spec.selected_side_channel, selected_bit=spec.selected_bit,
         fft_length=spec.fft_length, naccumulate=spec.naccumulate, nbits=spec.nbits,

@@ -23,22 +23,23 @@ def oracle_config(spec, convention):
                     spec.nbits, spec.dual_pol, convention)
 
 
-def make_gpu(spec, convention, sink, flags=0):
+def make_gpu(spec, convention, sink, flags=0, form=0):
     lay = G.DadaBufferLayout(spec.buffer_size, spec.heap_size, spec.n_side_channels)
     return G.GatedSpectrometer(lay, spec.selected_side_channel, spec.selected_bit, spec.fft_length,
                                spec.naccumulate, spec.nbits, 100.0, 100.0, sink,
                                input_type=G.DUAL_POL if spec.dual_pol else G.SINGLE_POL,
                                convention=G.REFERENCE if convention == "reference" else G.INTENDED,
-                               flags=flags)
+                               flags=flags, form=form)
 
 
 def run_both(spec, convention="intended", nblocks=6, kind="default", lost=0.0, seed=11, extra_bits=False,
-             flags=0, check_baselines=True):
+             flags=0, check_baselines=True, form=0, by_product=None):
     """Feeds nblocks blocks to both implementations; returns
-    (gpu_blocks, oracle_payloads, max_rel_err)."""
+    (gpu_blocks, oracle_payloads, max_rel_err).  by_product (a dict) collects
+    the worst error per Stokes product / gate."""
     cfg = oracle_config(spec, convention)
     sink = G.CollectingSink()
-    gpu = make_gpu(spec, convention, sink, flags)
+    gpu = make_gpu(spec, convention, sink, flags, form)
     orc = O.OracleSpectrometer(cfg)
     payloads = []
     try:
@@ -66,6 +67,9 @@ def run_both(spec, convention="intended", nblocks=6, kind="default", lost=0.0, s
                 assert np.array_equal(cnt, np.tile(np.stack([ref["n0"], ref["n1"]], 1), 4))
             err = O.rel_err(spec_f, ref["spec"], FLOOR)
             worst = max(worst, err)
+            if by_product is not None:
+                for key, v in O.rel_err_by_product(spec_f, ref["spec"], FLOOR).items():
+                    by_product[key] = max(by_product.get(key, 0.0), v)
             if flags & G.FLAG_SATURATION_RECORD:
                 sat = np.frombuffer(bytes(got[cfg.output_bytes:]), "<u8").reshape(cfg.n_out, 2)
                 assert np.array_equal(sat[:, 0], ref["sat0"]) and np.array_equal(sat[:, 1], ref["sat1"])

@@ -47,3 +47,49 @@ def test_tc_dft1024_tones_and_impulse():
     scale = np.abs(ref).max(axis=1, keepdims=True)
     assert (np.abs(got - ref) / scale).max() < 1e-4
     assert np.argmax(np.abs(got[1])) == 5 and np.argmax(np.abs(got[2])) == 24
+
+
+# ---------------------------------------------------------------- whole chain
+from psrdada_cpp_gb300 import synth  # noqa: E402
+from tests.gpu_helpers import run_both  # noqa: E402
+
+S = synth.StreamSpec
+# split-precision forms against the FP64 oracle: per-bin relative error (Stokes
+# products normalised by I, floor 1 % of the mean) within CHAIN_TOL (max) and
+# CHAIN_RMS (root mean square); counters, gate assignment and baselines
+# bit-exact as in the FP32 form.  A BF16 hi+lo operand keeps 2^-18 of its
+# value (8-bit mantissas), so each of the four DFT-32 stages adds ~1e-5 of the
+# spectrum's rms amplitude; a bin at the 1 % floor sees ~20x that in relative
+# power.  FP16 halves (11-bit mantissas) keep 2^-24: FP32-like.
+CHAIN_TOL = {G.FORM_BF16: 1e-3, G.FORM_FP16: 1e-4}
+CHAIN_RMS = {G.FORM_BF16: 1e-4, G.FORM_FP16: 1e-5}
+TC_CASES = [
+    # dual-pol 12-bit at 2^20 (both passes on the tensor cores), outliers at full scale
+    ("d12_n2p20", S("d12_n2p20", 12, True, 6144, 1, 1 << 21, 1 << 20, 2, diode_period_heaps=64), "c3"),
+    # single-pol 8-bit at 2^17: N1 = 1024 (pass A on the tensor cores), N2 = 128
+    ("s8_n2p17", S("s8_n2p17", 8, False, 4096, 1, 1 << 18, 1 << 17, 2, diode_period_heaps=5), "default"),
+    # dual-pol 10-bit at 2^16: N1 = 64, N2 = 1024 (pass B on the tensor cores), 2 blocks per output
+    ("d10_n2p16_nb2", S("d10_n2p16", 10, True, 5120, 1, 1 << 16, 1 << 16, 2, diode_period_heaps=3), "default"),
+]
+
+
+@pytest.mark.parametrize("form", [G.FORM_BF16, G.FORM_FP16])
+@pytest.mark.parametrize("name,spec,kind", TC_CASES, ids=[c[0] for c in TC_CASES])
+def test_tc_chain_matches_oracle(name, spec, kind, form):
+    from oracle import gspec_oracle as O
+    from tests.gpu_helpers import oracle_config, FLOOR
+    prod = {}
+    blocks, payloads, worst = run_both(spec, nblocks=6, kind=kind, lost=0.02, form=form, by_product=prod)
+    assert payloads, "no output block compared"
+    cfg = oracle_config(spec, "intended")
+    rms = max(O.rel_err(O.parse_output(bytes(b[:cfg.output_bytes]), cfg)[0], p["spec"], FLOOR, rms=True)
+              for b, p in zip(blocks, payloads))
+    print(f"{name} form={form} max rel err {worst:.3e} rms {rms:.3e} by product {prod}")
+    assert worst <= CHAIN_TOL[form], (worst, prod)
+    assert rms <= CHAIN_RMS[form], rms
+
+
+def test_tc_form_rejected_without_1024_pass():
+    lay = G.DadaBufferLayout(4096 * 16 + 16 * 8, 4096, 1)
+    with pytest.raises(G.GspecError):
+        G.GatedSpectrometer(lay, 0, 0, 4096, 4, 8, 1.0, 1.0, G.NullSink(), form=G.FORM_BF16)

@@ -18,7 +18,7 @@ ROOT = __import__("pathlib").Path(__file__).resolve().parents[1]
 
 STRUCTS = {
     "gspec_config": (GspecConfig, ["buffer_size", "naccumulate", "nbits", "device", "flags", "tune_units",
-                                   "tune_n1", "tune_scratch_mb", "stream_priority"]),
+                                   "tune_n1", "tune_scratch_mb", "stream_priority", "form"]),
     "gspec_info": (GspecInfo, ["nchans", "device_bytes", "kernel_launches"]),
     "gspec_server_config": (serving.GspecServerConfig, ["memory_budget", "device", "max_inflight",
                                                         "output_buffers", "inflight_bytes"]),
