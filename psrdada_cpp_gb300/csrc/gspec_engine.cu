@@ -265,9 +265,7 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
     f.N2 = h->N2;
     f.maxjobs = h->maxjobs;
     f.form = h->cfg.form;
-    f.tc_hi = h->d_tc_hi;
-    f.tc_lo = h->d_tc_lo;
-    f.tc_w = h->d_tc_w;
+    f.tc_img = reinterpret_cast<const uint4*>(h->d_tc_img);
     f.jobs = h->d_jobs;
     f.njobs = h->d_njobs;
     f.dc = h->d_dc;
@@ -318,7 +316,7 @@ void release(gspec_handle* h) {
   }
   void* ptrs[] = {h->d_sat_dev, h->d_baselines, h->d_pol_stats, h->d_tw,   h->d_tw1,   h->d_tw2,  h->d_twA,
                   h->d_twB,     h->d_partial,   h->d_scratch,   h->d_masks, h->d_flags, h->d_jobs, h->d_njobs,
-                  h->d_dc,      h->d_err,       h->d_tc_hi,     h->d_tc_lo, h->d_tc_w};
+                  h->d_dc,      h->d_err,       h->d_tc_hi,     h->d_tc_lo, h->d_tc_w, h->d_tc_img};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->h_err) cudaFreeHost(h->h_err);
@@ -474,7 +472,8 @@ uint64_t footprint(const gspec_handle* h) {
     t += sz(static_cast<uint64_t>(h->kchunk) * h->maxjobs * N * sizeof(float2));
     t += sz(h->n_out * h->maxjobs * sizeof(uint32_t)) + sz(h->n_out * sizeof(uint32_t)) +
          sz(2ull * h->n_out * sizeof(uint32_t));
-    if (h->cfg.form != GSPEC_FORM_FP32) t += 2 * sz(4096 * sizeof(uint16_t)) + sz(1024 * sizeof(float2));
+    if (h->cfg.form != GSPEC_FORM_FP32)
+      t += 2 * sz(4096 * sizeof(uint16_t)) + sz(1024 * sizeof(float2)) + sz(tc::kImageBytesHost);
   }
   return t;
 }
@@ -595,10 +594,12 @@ gspec_handle* gspec_create(const gspec_config* cfg, char* err, size_t err_len) {
     if (cfg->form != GSPEC_FORM_FP32) {
       if (!dalloc(h, &h->d_tc_hi, 4096 * sizeof(uint16_t), "tensor-core operand") ||
           !dalloc(h, &h->d_tc_lo, 4096 * sizeof(uint16_t), "tensor-core operand") ||
-          !dalloc(h, &h->d_tc_w, 1024 * sizeof(float2), "tensor-core twiddles"))
+          !dalloc(h, &h->d_tc_w, 1024 * sizeof(float2), "tensor-core twiddles") ||
+          !dalloc(h, &h->d_tc_img, tc::kImageBytesHost, "tensor-core image"))
         return bail("");
       if (!cuda_ok(h, tc::launch_tables(h->d_tc_hi, h->d_tc_lo, h->d_tc_w, cfg->form == GSPEC_FORM_BF16, h->proc),
-                   "tensor-core tables"))
+                   "tensor-core tables") ||
+          !cuda_ok(h, tc::launch_image(h->d_tc_hi, h->d_tc_lo, h->d_tc_w, h->d_tc_img, h->proc), "tensor-core image"))
         return bail("");
     }
   }

@@ -51,6 +51,7 @@ struct gspec_handle {
   uint16_t* d_tc_hi = nullptr;     // tensor-core form: DFT-32 operand halves
   uint16_t* d_tc_lo = nullptr;
   float2* d_tc_w = nullptr;        // W1024 twiddles
+  uint8_t* d_tc_img = nullptr;     // [B_hi | B_lo | W1024] in shared-memory layout
   uint32_t maxjobs = 0;
   int32_t heap_shift = -1;
   uint32_t* d_err = nullptr;       // set by kernels whose bounded waits gave up

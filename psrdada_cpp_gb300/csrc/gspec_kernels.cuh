@@ -47,9 +47,7 @@ struct FourStepParams {
   uint32_t* dc;                    // [n_out][2] frames without data per gate
   // tensor-core form (form != 0): DFT-32 operand halves and W1024 twiddles
   uint32_t form;                   // GSPEC_FORM_*
-  const uint16_t* tc_hi;
-  const uint16_t* tc_lo;
-  const float2* tc_w;
+  const uint4* tc_img;             // [B_hi | B_lo | W1024] in shared-memory layout
 };
 
 // Host-side launchers (gspec_kernels.cu).

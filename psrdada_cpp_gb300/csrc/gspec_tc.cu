@@ -47,6 +47,26 @@ cudaError_t launch_tables(uint16_t* hi, uint16_t* lo, float2* w1024, bool bf16, 
   return cudaGetLastError();
 }
 
+// The shared-memory image of [B_hi | B_lo | W1024] (canonical layout, pad
+// bytes zero) that every tensor-core CTA copies with 16-byte loads.
+__global__ void image_kernel(const uint16_t* hi, const uint16_t* lo, const float2* w, uint8_t* img) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < static_cast<int>(kImageBytes); i += gridDim.x * blockDim.x)
+    img[i] = 0;
+  __syncthreads();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 64 * 64; i += gridDim.x * blockDim.x) {
+    const int n = i >> 6, k = i & 63;
+    *reinterpret_cast<uint16_t*>(img + kmaj_off(n, k)) = hi[i];
+    *reinterpret_cast<uint16_t*>(img + kBBytes + kmaj_off(n, k)) = lo[i];
+  }
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < 1024; j += gridDim.x * blockDim.x)
+    reinterpret_cast<float2*>(img + 2 * kBBytes)[j] = w[j];
+}
+
+cudaError_t launch_image(const uint16_t* hi, const uint16_t* lo, const float2* w, uint8_t* img, cudaStream_t s) {
+  image_kernel<<<1, 256, 0, s>>>(hi, lo, w, img);
+  return cudaGetLastError();
+}
+
 // Test kernel: ntiles x 4 transforms of 1024 points, global in/out.
 template <bool BF16>
 __global__ void __launch_bounds__(128) dft1024_test_kernel(const float2* __restrict__ in, float2* __restrict__ out,
@@ -156,12 +176,17 @@ template <bool BF16> struct Scales {
   static constexpr float b1 = BF16 ? 1.f : 1.f / 64, b2 = BF16 ? 1.f : 1.f / 32;
 };
 
+__device__ __forceinline__ void load_image(char* dst, const uint4* __restrict__ img, int tid, int nthreads) {
+  uint4* d = reinterpret_cast<uint4*>(dst);
+  for (int i = tid; i < static_cast<int>(kImageBytes / 16); i += nthreads) d[i] = __ldg(img + i);
+}
+
 struct PassALayout {
   static constexpr size_t A = 0;
-  static constexpr size_t B = 2 * kABytes;
-  static constexpr size_t S = B + 2 * kBBytes;
-  static constexpr size_t W = S + static_cast<size_t>(4) * kColStride * sizeof(float2);
-  static constexpr size_t RED = W + 1024 * sizeof(float2);
+  static constexpr size_t B = 2 * kABytes;            // [B_hi | B_lo | W1024]: the image
+  static constexpr size_t W = B + 2 * kBBytes;
+  static constexpr size_t S = W + 1024 * sizeof(float2);
+  static constexpr size_t RED = S + static_cast<size_t>(4) * kColStride * sizeof(float2);
   static constexpr size_t BAR = RED + (kPassThreads / 32) * 12 * 8;
   static constexpr size_t BYTES = BAR + 16;
 };
@@ -205,8 +230,7 @@ __global__ void __launch_bounds__(kPassThreads, 2) tc_a_kernel(FourStepParams p)
   float bl[2 * NPOL];
 #pragma unroll
   for (int i = 0; i < 2 * NPOL; ++i) bl[i] = p.c.baselines[i];
-  load_dft32_operand(s.b_hi, s.b_lo, p.tc_hi, p.tc_lo, tid, kPassThreads);
-  for (int i = tid; i < 1024; i += kPassThreads) w[i] = p.tc_w[i];
+  load_image(smem + L::B, p.tc_img, tid, kPassThreads);
   if (tid == 0) {
     mbar_init(bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -279,10 +303,10 @@ struct PassBLayout {
   static constexpr int VALS = DUAL ? 8 : 2;
   static constexpr int BPT = (1024 + 1 + kPassThreads - 1) / kPassThreads;
   static constexpr size_t A = 0;                     // operands; the transformed rows ("work") alias them
-  static constexpr size_t B = 2 * kABytes;
-  static constexpr size_t STAGE = B + 2 * kBBytes;
-  static constexpr size_t W = STAGE + static_cast<size_t>(J) * 2 * 1024 * sizeof(float2);
-  static constexpr size_t JW = W + 1024 * sizeof(float2);
+  static constexpr size_t B = 2 * kABytes;            // [B_hi | B_lo | W1024]: the image
+  static constexpr size_t W = B + 2 * kBBytes;
+  static constexpr size_t STAGE = W + 1024 * sizeof(float2);
+  static constexpr size_t JW = STAGE + static_cast<size_t>(J) * 2 * 1024 * sizeof(float2);
   static constexpr size_t BAR = JW + 16;
   static constexpr size_t BYTES = BAR + 32;
   static_assert(static_cast<size_t>(4) * kRowStride * sizeof(float2) <= 2 * kABytes, "work fits the operands");
@@ -333,8 +357,7 @@ __global__ void __launch_bounds__(kPassThreads, 2) tc_b_kernel(FourStepParams p)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (tid < 32) tmem_alloc(tmem_slot, kTmemCols);
-  load_dft32_operand(s.b_hi, s.b_lo, p.tc_hi, p.tc_lo, tid, kPassThreads);
-  for (int i = tid; i < 1024; i += kPassThreads) w[i] = p.tc_w[i];
+  load_image(smem + L::B, p.tc_img, tid, kPassThreads);
   fence_before();
   __syncthreads();
   fence_after();

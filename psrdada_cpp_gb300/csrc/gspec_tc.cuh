@@ -34,6 +34,8 @@ constexpr uint32_t kSBO = 8 * kLBO;              // 8 K-chunks of 8 elements per
 constexpr uint32_t kABytes = 16 * kSBO;          // 128 rows x 64 bf16
 constexpr uint32_t kBBytes = 8 * kSBO;           // 64 rows x 64 bf16
 constexpr uint32_t kTmemCols = 64;               // 128 lanes x 64 fp32 accumulators
+constexpr uint32_t kImageBytes = 2 * kBBytes + 1024 * 8;   // [B_hi | B_lo | W1024] in shared-memory layout
+static_assert(kImageBytes == 2 * 9216 + 1024 * 8, "image size as declared for the host");
 constexpr uint32_t kWaitLimit = 1u << 22;
 
 __host__ __device__ constexpr uint32_t kmaj_off(uint32_t row, uint32_t k) {
