@@ -182,35 +182,48 @@ __device__ __forceinline__ void load_image(char* dst, const uint4* __restrict__ 
 }
 
 struct PassALayout {
-  static constexpr size_t A = 0;
-  static constexpr size_t B = 2 * kABytes;            // [B_hi | B_lo | W1024]: the image
-  static constexpr size_t W = B + 2 * kBBytes;
-  static constexpr size_t S = W + 1024 * sizeof(float2);
-  static constexpr size_t RED = S + static_cast<size_t>(4) * kColStride * sizeof(float2);
-  static constexpr size_t BAR = RED + (kPassThreads / 32) * 12 * 8;
-  static constexpr size_t BYTES = BAR + 16;
+  static constexpr int BC = 8;                          // columns per CTA: two tiles of 4
+  static constexpr int THREADS = 2 * kPassThreads;      // one 128-thread group per tile
+  static constexpr size_t A = 0;                        // per tile: operands, then its transformed columns
+  static constexpr size_t TILE = 2 * kABytes;
+  static constexpr size_t B = 2 * TILE;                 // [B_hi | B_lo | W1024]: the image
+  static constexpr size_t RED = B + kImageBytes;
+  static constexpr size_t BAR = RED + (THREADS / 32) * 12 * 8;
+  static constexpr size_t BYTES = BAR + 32;
+  static_assert(static_cast<size_t>(4) * kColStride * sizeof(float2) <= TILE, "columns fit the operands");
 };
 
-// grid.x = nk * maxjobs * (N2 / 4): (output spectrum, job, tile of 4 columns)
+// grid.x = nk * maxjobs * (N2 / 8): (output spectrum, job, 8 columns).  The
+// gather unpacks and gates each row's group of samples once and stores the
+// 8 kept columns straight into the stage-1 operands of the two tiles; each
+// 128-thread group then runs its tile's two tensor-core stages, and the
+// transformed columns (written over the operands) leave with the
+// W_N^(n2*k1) twiddle.
 template <int NBITS, bool DUAL, bool BF16>
-__global__ void __launch_bounds__(kPassThreads, 2) tc_a_kernel(FourStepParams p) {
-  constexpr int N1 = 1024, BC = 4;
+__global__ void __launch_bounds__(PassALayout::THREADS, 2) tc_a_kernel(FourStepParams p) {
+  constexpr int N1 = 1024;
+  using L = PassALayout;
+  constexpr int BC = L::BC, THREADS = L::THREADS;
   constexpr int G = Group<NBITS>::samples;
   constexpr int NPOL = DUAL ? 2 : 1;
   extern __shared__ __align__(1024) char smem[];
-  using L = PassALayout;
-  TileSmem s;
-  s.a_hi = smem + L::A;
-  s.a_lo = smem + L::A + kABytes;
-  s.b_hi = smem + L::B;
-  s.b_lo = smem + L::B + kBBytes;
-  float2* S = reinterpret_cast<float2*>(smem + L::S);
-  float2* w = reinterpret_cast<float2*>(smem + L::W);
-  unsigned long long* red = reinterpret_cast<unsigned long long*>(smem + L::RED);
+  const int tid = threadIdx.x;
+  const int grp = tid >> 7, gtid = tid & 127;
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L::BAR);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
-  s.w = w;
-  s.bar = bar;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 2);
+  unsigned long long* red = reinterpret_cast<unsigned long long*>(smem + L::RED);
+  auto tile_smem = [&](int g) {
+    TileSmem t;
+    t.a_hi = smem + L::A + g * L::TILE;
+    t.a_lo = t.a_hi + kABytes;
+    t.b_hi = smem + L::B;
+    t.b_lo = smem + L::B + kBBytes;
+    t.w = reinterpret_cast<const float2*>(smem + L::B + 2 * kBBytes);
+    t.bar = bar + g;
+    return t;
+  };
+  TileSmem s = tile_smem(grp);
+  const TileSmem s0 = tile_smem(0), s1 = tile_smem(1);
 
   const uint32_t N2 = p.N2;
   const uint32_t N = N1 * N2;
@@ -225,25 +238,27 @@ __global__ void __launch_bounds__(kPassThreads, 2) tc_a_kernel(FourStepParams p)
   const uint32_t frA = k * p.c.nacc + fa;
   const uint32_t frB = k * p.c.nacc + fb;
   const uint32_t c0 = tile * BC;
-  const int tid = threadIdx.x;
 
   float bl[2 * NPOL];
 #pragma unroll
   for (int i = 0; i < 2 * NPOL; ++i) bl[i] = p.c.baselines[i];
-  load_image(smem + L::B, p.tc_img, tid, kPassThreads);
+  load_image(smem + L::B, p.tc_img, tid, THREADS);
   if (tid == 0) {
     mbar_init(bar, 1);
+    mbar_init(bar + 1, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (tid < 32) tmem_alloc(tmem_slot, kTmemCols);
+  if (tid < 32) tmem_alloc(tmem_slot, 2 * kTmemCols);
 
-  // unpack + gate this tile's 4 columns of all N1 rows (one group per row)
-  const uint32_t gbase = (c0 / G) * G;
+  // unpack + gate the 8 columns of every row (one group per row) into the
+  // stage-1 operands of both tiles
+  constexpr float sc1 = Scales<BF16>::a1, sc2 = Scales<BF16>::a2;
+  const uint32_t gbase = G <= BC ? c0 : (c0 / G) * G;
   const int keep0 = static_cast<int>(c0 - gbase);
-  const bool count_stats = c0 == gbase;
+  const bool count_stats = G <= BC || c0 == gbase;
   const uint32_t sg_a = count_stats ? (DUAL ? (1u << ga) : 3u) : 0u;
   GateStats st[NPOL];
-  for (int n1 = tid; n1 < N1; n1 += kPassThreads) {
+  for (int n1 = tid; n1 < N1; n1 += THREADS) {
     const uint32_t off = N2 * n1 + gbase;
     float re[G], im[G];
     if constexpr (DUAL) {
@@ -261,27 +276,29 @@ __global__ void __launch_bounds__(kPassThreads, 2) tc_a_kernel(FourStepParams p)
       }
     }
 #pragma unroll
-    for (int e = 0; e < G; ++e)
-      if (e >= keep0 && e < keep0 + BC) S[(e - keep0) * kColStride + spad(n1)] = make_float2(re[e], im[e]);
+    for (int e = 0; e < G; ++e) {
+      const int col = e - keep0;
+      if (col >= 0 && col < BC) put_stage1<BF16>(col < 4 ? s0 : s1, col & 3, n1, make_float2(re[e], im[e]), sc1);
+    }
   }
   fence_before();
   __syncthreads();
   fence_after();
-  s.tmem = *tmem_slot;
+  s.tmem = *tmem_slot + grp * kTmemCols;
   uint32_t phase = 0;
-  const bool ok = dft1024_tile<BF16>(
-      s, phase, tid, [&](int t, int n) { return S[t * kColStride + spad(n)]; },
-      [&](int t, int k1, float2 v) { S[t * kColStride + spad(k1)] = v; }, [] {}, Scales<BF16>::a1,
-      Scales<BF16>::a2);
-  if (!ok && tid == 0 && p.c.dev_err) atomicExch(p.c.dev_err, 3u);
+  float2* S = reinterpret_cast<float2*>(s.a_hi);          // this tile's columns after the transform
+  const bool ok = dft1024_stages<BF16>(
+      s, phase, gtid, [&](int t, int k1, float2 v) { S[t * kColStride + spad(k1)] = v; }, [] {}, sc1, sc2);
+  if (!ok && gtid == 0 && p.c.dev_err) atomicExch(p.c.dev_err, 3u);
   __syncthreads();
   // twiddle W_N^(n2*k1) and store Y[k1][n2] (as the FP32 pass)
   float2* dst = p.scratch + (static_cast<size_t>(kk) * p.maxjobs + j) * N;
   {
-    constexpr int KS = kPassThreads / BC;
+    constexpr int KS = THREADS / BC;
     constexpr int PPT = N1 / KS;
     const int col = tid % BC;
     const uint32_t n2 = c0 + col;
+    const float2* Sc = reinterpret_cast<const float2*>(smem + L::A + (col >> 2) * L::TILE) + (col & 3) * kColStride;
     auto exact = [&](uint32_t m) { return cmul(__ldg(&p.twA[m >> 10]), __ldg(&p.twB[m & 1023])); };
     const float2 D = exact(n2 * KS);
     float2 W = make_float2(1.f, 0.f);
@@ -289,12 +306,12 @@ __global__ void __launch_bounds__(kPassThreads, 2) tc_a_kernel(FourStepParams p)
     for (int i = 0; i < PPT; ++i) {
       const int k1 = tid / BC + KS * i;
       W = (i & 3) == 0 ? exact(n2 * static_cast<uint32_t>(k1)) : cmul(W, D);
-      dst[static_cast<size_t>(k1) * N2 + n2] = cmul(S[col * kColStride + spad(k1)], W);
+      dst[static_cast<size_t>(k1) * N2 + n2] = cmul(Sc[spad(k1)], W);
     }
   }
   commit_stats<NPOL>(p.c, st, k, (DUAL ? 8 : 2) * static_cast<int>(N / 2 + 1), red);
   fence_after();
-  if (tid < 32) tmem_dealloc(s.tmem, kTmemCols);
+  if (tid < 32) tmem_dealloc(*tmem_slot, 2 * kTmemCols);
 }
 
 template <bool DUAL>
@@ -487,10 +504,11 @@ __global__ void __launch_bounds__(kPassThreads, 2) tc_b_kernel(FourStepParams p)
 }
 
 template <class K>
-static cudaError_t run_tc(K kern, unsigned grid, size_t smem, const FourStepParams& p, cudaStream_t s) {
+static cudaError_t run_tc(K kern, unsigned grid, size_t smem, const FourStepParams& p, cudaStream_t s,
+                          int threads = kPassThreads) {
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   if (e != cudaSuccess) return e;
-  kern<<<grid, kPassThreads, smem, s>>>(p);
+  kern<<<grid, threads, smem, s>>>(p);
   return cudaGetLastError();
 }
 
@@ -498,15 +516,15 @@ template <bool BF16>
 static cudaError_t launch_pass(int pass, int nbits, bool dual, const FourStepParams& p, cudaStream_t s) {
   if (pass == 0) {
     if (p.N1 != 1024) return cudaErrorInvalidValue;
-    const unsigned grid = p.nk * p.maxjobs * (p.N2 / 4);
+    const unsigned grid = p.nk * p.maxjobs * (p.N2 / PassALayout::BC);
     const size_t sm = PassALayout::BYTES;
     switch (nbits * 2 + (dual ? 1 : 0)) {
-      case 16: return run_tc(tc_a_kernel<8, false, BF16>, grid, sm, p, s);
-      case 17: return run_tc(tc_a_kernel<8, true, BF16>, grid, sm, p, s);
-      case 20: return run_tc(tc_a_kernel<10, false, BF16>, grid, sm, p, s);
-      case 21: return run_tc(tc_a_kernel<10, true, BF16>, grid, sm, p, s);
-      case 24: return run_tc(tc_a_kernel<12, false, BF16>, grid, sm, p, s);
-      case 25: return run_tc(tc_a_kernel<12, true, BF16>, grid, sm, p, s);
+      case 16: return run_tc(tc_a_kernel<8, false, BF16>, grid, sm, p, s, PassALayout::THREADS);
+      case 17: return run_tc(tc_a_kernel<8, true, BF16>, grid, sm, p, s, PassALayout::THREADS);
+      case 20: return run_tc(tc_a_kernel<10, false, BF16>, grid, sm, p, s, PassALayout::THREADS);
+      case 21: return run_tc(tc_a_kernel<10, true, BF16>, grid, sm, p, s, PassALayout::THREADS);
+      case 24: return run_tc(tc_a_kernel<12, false, BF16>, grid, sm, p, s, PassALayout::THREADS);
+      case 25: return run_tc(tc_a_kernel<12, true, BF16>, grid, sm, p, s, PassALayout::THREADS);
     }
     return cudaErrorInvalidValue;
   }

@@ -145,27 +145,23 @@ __device__ __forceinline__ void issue_stage(const TileSmem& s) {
 
 __device__ __forceinline__ float2 scale2(float2 v, float f) { return make_float2(v.x * f, v.y * f); }
 
-// DFT-1024 of four transforms by the 128 threads of the calling group
-// (thread tid of the group; all threads of the block call it together).
-// x(t, n) returns input n of transform t; y(t, k, v) takes output k.
-// mid() runs on every thread once the inputs have been read (after the
-// first barrier), e.g. to start loading the next inputs.  sc1 and sc2 scale
-// the operands of the two stages by powers of two (the FP16 form keeps them
-// in range); the outputs are scaled back exactly.  Returns false if a
-// bounded wait on the tensor cores gave up.
-template <bool BF16, class X, class Y, class M>
-__device__ __forceinline__ bool dft1024_tile(const TileSmem& s, uint32_t& phase, int tid, X x, Y y, M mid,
-                                             float sc1 = 1.f, float sc2 = 1.f) {
+// Stage-1 operand of input x[t][n] (n = 32a + b) in row 32t + b, K = 2a + r,
+// stored by whoever produces the value (scaled by sc1, split hi/lo).
+template <bool BF16>
+__device__ __forceinline__ void put_stage1(const TileSmem& s, int t, int n, float2 v, float sc1) {
+  uint32_t hi, lo;
+  split2<BF16>(scale2(v, sc1), hi, lo);
+  const uint32_t off = kmaj_off(32 * t + (n & 31), 2 * (n >> 5));
+  *reinterpret_cast<uint32_t*>(s.a_hi + off) = hi;
+  *reinterpret_cast<uint32_t*>(s.a_lo + off) = lo;
+}
+
+// The two tensor-core stages of a tile whose stage-1 operands are in place
+// (see dft1024_tile); every thread of the block calls it.
+template <bool BF16, class Y, class M>
+__device__ __forceinline__ bool dft1024_stages(const TileSmem& s, uint32_t& phase, int tid, Y y, M mid, float sc1,
+                                               float sc2) {
   const int t = tid >> 5, lane = tid & 31;
-  // stage 1: row tid = (t, b = lane) holds x[32a + b], a = 0..31
-#pragma unroll
-  for (int kc = 0; kc < 8; ++kc) {
-    uint32_t h[4], l[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) split2<BF16>(scale2(x(t, 32 * (4 * kc + j) + lane), sc1), h[j], l[j]);
-    *reinterpret_cast<uint4*>(s.a_hi + kmaj_off(tid, 8 * kc)) = make_uint4(h[0], h[1], h[2], h[3]);
-    *reinterpret_cast<uint4*>(s.a_lo + kmaj_off(tid, 8 * kc)) = make_uint4(l[0], l[1], l[2], l[3]);
-  }
   fence_async_smem();
   __syncthreads();
   mid();
@@ -213,6 +209,30 @@ __device__ __forceinline__ bool dft1024_tile(const TileSmem& s, uint32_t& phase,
   for (int d = 0; d < 16; ++d) y(t, lane + 32 * (d + 16), make_float2(v[2 * d] * inv, v[2 * d + 1] * inv));
   fence_before();
   return ok;
+}
+
+// DFT-1024 of four transforms by the 128 threads of the calling group
+// (thread tid of the group; all threads of the block call it together).
+// x(t, n) returns input n of transform t; y(t, k, v) takes output k.
+// mid() runs on every thread once the inputs have been read (after the
+// first barrier), e.g. to start loading the next inputs.  sc1 and sc2 scale
+// the operands of the two stages by powers of two (the FP16 form keeps them
+// in range); the outputs are scaled back exactly.  Returns false if a
+// bounded wait on the tensor cores gave up.
+template <bool BF16, class X, class Y, class M>
+__device__ __forceinline__ bool dft1024_tile(const TileSmem& s, uint32_t& phase, int tid, X x, Y y, M mid,
+                                             float sc1 = 1.f, float sc2 = 1.f) {
+  const int t = tid >> 5, lane = tid & 31;
+  // stage 1: row tid = (t, b = lane) holds x[32a + b], a = 0..31
+#pragma unroll
+  for (int kc = 0; kc < 8; ++kc) {
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) split2<BF16>(scale2(x(t, 32 * (4 * kc + j) + lane), sc1), h[j], l[j]);
+    *reinterpret_cast<uint4*>(s.a_hi + kmaj_off(tid, 8 * kc)) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4*>(s.a_lo + kmaj_off(tid, 8 * kc)) = make_uint4(l[0], l[1], l[2], l[3]);
+  }
+  return dft1024_stages<BF16>(s, phase, tid, y, mid, sc1, sc2);
 }
 
 // Copies the DFT-32 operand halves (logical [n][k] 64 x 64 16-bit arrays in
