@@ -141,6 +141,9 @@ __global__ void __launch_bounds__(PassACfg<N1>::THREADS) fourstep_a_kernel(FourS
 #ifndef GSPEC_PASSB_THREADS
 #define GSPEC_PASSB_THREADS 128
 #endif
+#ifndef GSPEC_PASSB_STAGES
+#define GSPEC_PASSB_STAGES 2
+#endif
 
 template <int N2, bool DUAL>
 struct PassBCfg {
@@ -156,14 +159,15 @@ struct PassBCfg {
   static constexpr size_t WORK_BYTES = static_cast<size_t>(2 * J) * STRIDE * sizeof(float2);
   static constexpr size_t TW_BYTES = static_cast<size_t>(tw_size(N2)) * sizeof(float2);
   static constexpr size_t JW_BYTES = ((J * sizeof(uint32_t)) + 15) / 16 * 16;
-  static constexpr size_t SMEM = 2 * STAGE_BYTES + WORK_BYTES + TW_BYTES + JW_BYTES + 2 * sizeof(uint64_t);
+  static constexpr int NST = GSPEC_PASSB_STAGES;     // TMA stages: NST - 1 groups ahead
+  static constexpr size_t SMEM = NST * STAGE_BYTES + WORK_BYTES + TW_BYTES + JW_BYTES + NST * sizeof(uint64_t);
 };
 
 
 // grid.x = nk * N1/2: unit (output spectrum k, row pair rp).  J jobs are
 // transformed together (2*T2 threads each).  Their rows arrive by TMA bulk
-// copies into one of two staging buffers while the previous group is
-// transformed; the first FFT pass reads the staging buffer.  Thread t owns
+// copies into one of NST staging buffers, NST - 1 groups ahead of the group
+// being transformed; the first FFT pass reads the staging buffer.  Thread t owns
 // output slots a = t + THREADS*i of the pair and keeps their power / Stokes
 // sums in registers over all jobs of the spectrum, adding the jobs in
 // order, so the result does not depend on scheduling.
@@ -173,14 +177,15 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, 2) fourstep_b_ker
   constexpr int J = Cfg::J;
   constexpr int BPT = Cfg::BPT;
   constexpr int VALS = Cfg::VALS;
+  constexpr int NST = Cfg::NST;
   constexpr uint32_t kRowBytes = N2 * sizeof(float2);
   extern __shared__ float4 smem_f4[];
   char* base = reinterpret_cast<char*>(smem_f4);
-  float2* stage = reinterpret_cast<float2*>(base);                         // [2][J][2][N2]
-  float2* work = reinterpret_cast<float2*>(base + 2 * Cfg::STAGE_BYTES);   // [J][2][STRIDE]
-  float2* tws = reinterpret_cast<float2*>(base + 2 * Cfg::STAGE_BYTES + Cfg::WORK_BYTES);
-  uint32_t* jw = reinterpret_cast<uint32_t*>(base + 2 * Cfg::STAGE_BYTES + Cfg::WORK_BYTES + Cfg::TW_BYTES);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(base + 2 * Cfg::STAGE_BYTES + Cfg::WORK_BYTES + Cfg::TW_BYTES +
+  float2* stage = reinterpret_cast<float2*>(base);                           // [NST][J][2][N2]
+  float2* work = reinterpret_cast<float2*>(base + NST * Cfg::STAGE_BYTES);   // [J][2][STRIDE]
+  float2* tws = reinterpret_cast<float2*>(base + NST * Cfg::STAGE_BYTES + Cfg::WORK_BYTES);
+  uint32_t* jw = reinterpret_cast<uint32_t*>(base + NST * Cfg::STAGE_BYTES + Cfg::WORK_BYTES + Cfg::TW_BYTES);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + NST * Cfg::STAGE_BYTES + Cfg::WORK_BYTES + Cfg::TW_BYTES +
                                               Cfg::JW_BYTES);
 
   const uint32_t N1 = p.N1;
@@ -200,8 +205,8 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, 2) fourstep_b_ker
   const uint32_t* jobs = p.jobs + k * p.maxjobs;
   const uint32_t ngroups = (njobs + J - 1) / J;
   if (tid == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+#pragma unroll
+    for (int i = 0; i < NST; ++i) mbar_init(&bar[i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   load_twiddles<N2>(tws, p.tw2);
@@ -218,8 +223,12 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, 2) fourstep_b_ker
       bulk_g2s(dst + N2, seq + static_cast<size_t>(rowB) * N2, kRowBytes, &bar[s]);
     }
   };
-  if (tid == 0 && ngroups > 0) issue(0, 0);
+  if (tid == 0)
+    for (uint32_t g = 0; g + 1 < static_cast<uint32_t>(NST) && g < ngroups; ++g) issue(g, static_cast<int>(g));
 
+  // job words one group ahead: the global load of group g + 1 is in flight
+  // while group g is transformed
+  uint32_t next_job = (tid < J && static_cast<uint32_t>(tid) < njobs) ? jobs[tid] : 0u;
   float acc[BPT][VALS];
 #pragma unroll
   for (int i = 0; i < BPT; ++i)
@@ -227,15 +236,16 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, 2) fourstep_b_ker
     for (int v = 0; v < VALS; ++v) acc[i][v] = 0.f;
 
   for (uint32_t g = 0; g < ngroups; ++g) {
-    const int s = g & 1;
-    if (tid == 0 && g + 1 < ngroups) issue(g + 1, s ^ 1);
-    const bool ok = mbar_wait(&bar[s], (g >> 1) & 1u, 1u << 24);
+    const int s = static_cast<int>(g % NST);
+    // the stage of group g + NST - 1 held group g - 1, done at the last barrier
+    if (tid == 0 && g + NST - 1 < ngroups) issue(g + NST - 1, static_cast<int>((g + NST - 1) % NST));
+    const bool ok = mbar_wait(&bar[s], (g / NST) & 1u, 1u << 24);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) {
         if (p.c.dev_err) atomicExch(p.c.dev_err, 2u);
         // give the copies still in flight a bounded chance to land before exit
-        mbar_wait(&bar[s], (g >> 1) & 1u, 1u << 20);
-        if (g + 1 < ngroups) mbar_wait(&bar[s ^ 1], ((g + 1) >> 1) & 1u, 1u << 20);
+        for (uint32_t h = g; h < g + NST && h < ngroups; ++h)
+          mbar_wait(&bar[h % NST], (h / NST) & 1u, 1u << 20);
       }
       __syncthreads();
       break;
@@ -243,7 +253,8 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, 2) fourstep_b_ker
     const uint32_t j0 = g * J;
     const int nq = static_cast<int>(min(static_cast<uint32_t>(J), njobs - j0));
     const bool active = q < nq;
-    if (tid < nq) jw[tid] = jobs[j0 + tid];
+    if (tid < nq) jw[tid] = next_job;
+    if (tid < J && j0 + J + tid < njobs) next_job = jobs[j0 + J + tid];
     {
       const int r = lt / Cfg::T2;
       const int t = lt - r * Cfg::T2;

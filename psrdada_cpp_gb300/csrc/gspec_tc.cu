@@ -394,6 +394,9 @@ __global__ void __launch_bounds__(kPassThreads, 2) tc_b_kernel(FourStepParams p)
   };
   if (tid == 0 && ngroups > 0) issue(0);
 
+  // job words one group ahead: the global load of group g + 1 is in flight
+  // while group g is transformed
+  uint32_t next_job = (tid < J && static_cast<uint32_t>(tid) < njobs) ? jobs[tid] : 0u;
   float acc[BPT][VALS];
 #pragma unroll
   for (int i = 0; i < BPT; ++i)
@@ -414,7 +417,8 @@ __global__ void __launch_bounds__(kPassThreads, 2) tc_b_kernel(FourStepParams p)
     }
     const uint32_t j0 = g * J;
     const int nq = static_cast<int>(min(static_cast<uint32_t>(J), njobs - j0));
-    if (tid < nq) jw[tid] = jobs[j0 + tid];
+    if (tid < nq) jw[tid] = next_job;
+    if (tid < J && j0 + J + tid < njobs) next_job = jobs[j0 + J + tid];
     mma_ok = dft1024_tile<BF16>(
                  s, phase, tid, [&](int t, int n) { return stage[t * N2 + n]; },
                  [&](int t, int k2, float2 v) { work[t * kRowStride + spad(k2)] = v; },
