@@ -476,7 +476,12 @@ def run_batch(args):
     in_bytes = sum(s.buffer_size for s in specs)
     stream = torch.cuda.current_stream(dev)
     sp = stream.cuda_stream
-    bt = G.Batch([G.make_config(s, device=local, tune=tunes[s.name]) for s in specs])
+    # the tensor-core forms apply to members with a 1024-point four-step pass
+    form = {"fp32": G.FORM_FP32, "bf16": G.FORM_BF16, "fp16": G.FORM_FP16}[args.form]
+    forms = {s.name: (form if (1 << 16) <= s.fft_length <= (1 << 20) else G.FORM_FP32) for s in specs}
+    if form != G.FORM_FP32:
+        tunes = {k: ({} if forms[k] != G.FORM_FP32 else v) for k, v in tunes.items()}
+    bt = G.Batch([G.make_config(s, device=local, tune=tunes[s.name], form=forms[s.name]) for s in specs])
     for i, h in enumerate(host):
         bt.set_input(i, h, sp)
     torch.cuda.synchronize(dev)
@@ -509,7 +514,7 @@ def run_batch(args):
         lay = G.DadaBufferLayout(s.buffer_size, s.heap_size, s.n_side_channels)
         g = G.GatedSpectrometer(lay, 0, 0, s.fft_length, s.naccumulate, s.nbits, 1.0, 1.0, G.NullSink(),
                                 input_type=G.DUAL_POL if s.dual_pol else G.SINGLE_POL, device=local,
-                                flags=G.FLAG_NO_HOST_BUFFERS, tune=tunes[s.name])
+                                flags=G.FLAG_NO_HOST_BUFFERS, tune=tunes[s.name], form=forms[s.name])
         seq.append(g)
         d_out.append(torch.zeros(int(g.info().output_bytes), dtype=torch.uint8, device=dev))
     d_in = [torch.from_numpy(h).to(dev) for h in host]
@@ -529,7 +534,9 @@ def run_batch(args):
         g.close()
     del d_in, d_out
 
-    # end to end: pinned host blocks in, completed outputs out, every step
+    # end to end: pinned host blocks in, completed outputs out, every step.
+    # The blocks of step k + 1 go in on a copy stream while step k runs (the
+    # batch alternates two input buffers); outputs leave on the compute stream.
     pinned = []
     for h in host:
         t = torch.empty(h.size, dtype=torch.uint8, pin_memory=True)
@@ -537,18 +544,32 @@ def run_batch(args):
         pinned.append(t)
     outs = [torch.empty(int(bt.info(i).output_bytes), dtype=torch.uint8, pin_memory=True) for i in range(bt.n)]
     ke = max(4, min(steps, 64))
+    copy_stream = torch.cuda.Stream(dev)
+    cs = copy_stream.cuda_stream
+    copied = [torch.cuda.Event() for _ in range(ke)]
+    ran = [torch.cuda.Event() for _ in range(ke)]
     d2h = 0
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
-    for _ in range(ke):
-        for i, p in enumerate(pinned):
-            bt.set_input(i, p, sp)
+
+    def put(k):
+        if k >= 2:
+            copy_stream.wait_event(ran[k - 2])          # the buffer was last read by step k - 2
+        for i, p_ in enumerate(pinned):
+            bt.set_input(i, p_, cs)
+        copied[k].record(copy_stream)
+
+    put(0)
+    for k in range(ke):
+        stream.wait_event(copied[k])
         bt.run(sp)
+        ran[k].record(stream)
+        if k + 1 < ke:
+            put(k + 1)
         for i in range(bt.n):
-            ptr, n, complete = bt.output(i)
+            _, n, complete = bt.output(i)
             if complete:
-                bt._lib.gspec_batch_read_output(bt._b, i, __import__("ctypes").c_void_p(outs[i].data_ptr()), n,
-                                                __import__("ctypes").c_void_p(sp))
+                bt.copy_output(i, outs[i], sp)
                 d2h += n
     torch.cuda.synchronize(dev)
     e2e_s = time.perf_counter() - t0
@@ -560,13 +581,15 @@ def run_batch(args):
             "ms_per_step": round(ms / steps, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": "uneven_streams_16_seed3", "streams": [s.name for s in specs],
-                       "samples_per_step": samples_per_step, "input_bytes_per_step": in_bytes, "form": "fp32",
+                       "samples_per_step": samples_per_step, "input_bytes_per_step": in_bytes, "form": args.form,
+                       "forms": {k: int(v) for k, v in forms.items()},
                        "schedules": tunes, "tune_seconds": round(t_tune, 1),
                        "l2": "inputs larger than L2: the 16 members' blocks total %d B" % in_bytes},
             "sequential_no_graph": {"value": round(seq_value, 3), "unit": UNIT, "steps": ks},
             "e2e": {"value": round(samples_per_step * ke / e2e_s / 1e9, 3), "unit": UNIT,
                     "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": int(d2h / ke), "steps": ke,
-                    "api": "Batch.set_input (pinned) -> gspec_batch_run -> gspec_batch_read_output"},
+                    "api": "Batch.set_input (pinned, copy stream, one step ahead) -> gspec_batch_run -> "
+                           "gspec_batch_copy_output (pinned)"},
             "gpu_launches": int(kernels * steps), "kernels_per_graph": int(kernels),
             "clocks": clocks.summary(tw0, tw1),
         }

@@ -274,7 +274,10 @@ gspec_batch* gspec_batch_create(const gspec_config* cfgs, int n, char* err, size
 void gspec_batch_destroy(gspec_batch* b);
 int gspec_batch_size(const gspec_batch* b);
 int gspec_batch_get_info(const gspec_batch* b, int i, gspec_info* info);
-/* Device input block of member i (buffer_size bytes), read by the next run. */
+/* Device input block of member i (buffer_size bytes) read by the next run.
+ * Every member has two input buffers and runs alternate between them: the
+ * blocks of step k + 1 can be copied in while step k runs, ordered after
+ * step k - 1 (the last run that read the same buffer). */
 void* gspec_batch_input(gspec_batch* b, int i);
 /* Copies one block (host or device memory, buffer_size bytes) into member
  * i's input on the caller's stream. */
@@ -283,6 +286,8 @@ int gspec_batch_set_input(gspec_batch* b, int i, const void* src, size_t bytes, 
  * saturation record) to dst (host or device memory) on the caller's stream
  * and waits for the copy. */
 int gspec_batch_read_output(gspec_batch* b, int i, void* dst, size_t bytes, void* cuda_stream);
+/* The same copy enqueued on the caller's stream without waiting. */
+int gspec_batch_copy_output(gspec_batch* b, int i, void* dst, size_t bytes, void* cuda_stream);
 /* Device output accumulator of member i (output layout without the
  * saturation record) and whether the last run completed it. */
 int gspec_batch_output(gspec_batch* b, int i, void** d_out, uint64_t* bytes, int* complete);

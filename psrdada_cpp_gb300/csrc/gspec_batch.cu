@@ -10,7 +10,10 @@
 // phase_i clears member i's output accumulator when its device block counter
 // starts a new output block (counter % n_blocks == 0) and count_i advances the
 // counter, so the same graph serves every step of members whose n_blocks
-// differ.  Later runs replay the instantiated graph with one launch.
+// differ.  Each member has two input buffers and there is one graph per
+// buffer; runs alternate between them, so the next step's blocks can be
+// copied in while the current step runs.  Later runs replay the
+// instantiated graphs with one launch each.
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -43,8 +46,9 @@ struct gspec_batch {
   std::vector<cudaStream_t> branch;
   std::vector<cudaEvent_t> join;
   cudaEvent_t fork = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph[2] = {nullptr, nullptr};      // one per input buffer
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  int slot = 0;                                    // input buffer the next run reads
   uint64_t kernels_per_step = 0;
   uint64_t steps = 0;
   std::string err;
@@ -59,8 +63,10 @@ bool bok(gspec_batch* b, cudaError_t e, const char* what) {
 }
 
 void batch_free(gspec_batch* b) {
-  if (b->exec) cudaGraphExecDestroy(b->exec);
-  if (b->graph) cudaGraphDestroy(b->graph);
+  for (int i = 0; i < 2; ++i) {
+    if (b->exec[i]) cudaGraphExecDestroy(b->exec[i]);
+    if (b->graph[i]) cudaGraphDestroy(b->graph[i]);
+  }
   for (auto* h : b->h) gspec_destroy(h);
   for (auto s : b->branch) cudaStreamDestroy(s);
   for (auto e : b->join) cudaEventDestroy(e);
@@ -69,8 +75,9 @@ void batch_free(gspec_batch* b) {
   if (b->d_count) cudaFree(b->d_count);
 }
 
-// Records one step of every member into b->capture (being captured).
-bool record_step(gspec_batch* b) {
+// Records one step of every member, reading input buffer `slot`, into
+// b->capture (being captured).
+bool record_step(gspec_batch* b, int slot) {
   if (!bok(b, cudaEventRecord(b->fork, b->capture), "fork")) return false;
   for (size_t i = 0; i < b->h.size(); ++i) {
     gspec_handle* h = b->h[i];
@@ -84,7 +91,7 @@ bool record_step(gspec_batch* b) {
         b->d_count + i, static_cast<uint32_t>(h->n_blocks), reinterpret_cast<uint2*>(h->d_out[0]), n8,
         reinterpret_cast<uint2*>(h->d_sat[0]), s8);
     if (!bok(b, cudaGetLastError(), "phase kernel")) return false;
-    if (!bok(b, gspec_engine::run_chain(h, h->d_in[0], h->d_out[0], h->d_sat[0], s), "chain")) return false;
+    if (!bok(b, gspec_engine::run_chain(h, h->d_in[slot], h->d_out[0], h->d_sat[0], s), "chain")) return false;
     batch_count_kernel<<<1, 1, 0, s>>>(b->d_count + i);
     if (!bok(b, cudaGetLastError(), "count kernel")) return false;
     if (!bok(b, cudaEventRecord(b->join[i], s), "join") ||
@@ -94,9 +101,9 @@ bool record_step(gspec_batch* b) {
   return true;
 }
 
-bool build_graph(gspec_batch* b) {
+bool build_graph(gspec_batch* b, int slot) {
   if (!bok(b, cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal), "begin capture")) return false;
-  const bool rec = record_step(b);
+  const bool rec = record_step(b, slot);
   cudaGraph_t g = nullptr;
   const cudaError_t e = cudaStreamEndCapture(b->capture, &g);
   if (!rec) {
@@ -104,7 +111,7 @@ bool build_graph(gspec_batch* b) {
     return false;
   }
   if (!bok(b, e, "end capture")) return false;
-  b->graph = g;
+  b->graph[slot] = g;
   size_t n = 0;
   if (!bok(b, cudaGraphGetNodes(g, nullptr, &n), "graph nodes")) return false;
   std::vector<cudaGraphNode_t> nodes(n);
@@ -114,7 +121,7 @@ bool build_graph(gspec_batch* b) {
     cudaGraphNodeType t;
     if (cudaGraphNodeGetType(node, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++b->kernels_per_step;
   }
-  return bok(b, cudaGraphInstantiate(&b->exec, g, 0), "instantiate");
+  return bok(b, cudaGraphInstantiate(&b->exec[slot], g, 0), "instantiate");
 }
 
 }  // namespace
@@ -182,7 +189,7 @@ int gspec_batch_get_info(const gspec_batch* b, int i, gspec_info* info) {
 
 void* gspec_batch_input(gspec_batch* b, int i) {
   if (!b || i < 0 || i >= static_cast<int>(b->h.size())) return nullptr;
-  return b->h[i]->d_in[0];
+  return b->h[i]->d_in[b->slot];
 }
 
 int gspec_batch_set_input(gspec_batch* b, int i, const void* src, size_t bytes, void* cuda_stream) {
@@ -193,7 +200,7 @@ int gspec_batch_set_input(gspec_batch* b, int i, const void* src, size_t bytes, 
              std::to_string(h->cfg.buffer_size);
     return GSPEC_STOP;
   }
-  return bok(b, cudaMemcpyAsync(h->d_in[0], src, bytes, cudaMemcpyDefault, static_cast<cudaStream_t>(cuda_stream)),
+  return bok(b, cudaMemcpyAsync(h->d_in[b->slot], src, bytes, cudaMemcpyDefault, static_cast<cudaStream_t>(cuda_stream)),
              "input copy")
              ? GSPEC_OK
              : GSPEC_ERR_CUDA;
@@ -208,6 +215,16 @@ int gspec_batch_read_output(gspec_batch* b, int i, void* dst, size_t bytes, void
       !bok(b, cudaStreamSynchronize(s), "output copy"))
     return GSPEC_ERR_CUDA;
   return GSPEC_OK;
+}
+
+int gspec_batch_copy_output(gspec_batch* b, int i, void* dst, size_t bytes, void* cuda_stream) {
+  if (!b || !dst || i < 0 || i >= static_cast<int>(b->h.size())) return GSPEC_ERR_ARG;
+  gspec_handle* h = b->h[i];
+  if (bytes > h->out_bytes) return GSPEC_ERR_ARG;
+  return bok(b, cudaMemcpyAsync(dst, h->d_out[0], bytes, cudaMemcpyDefault, static_cast<cudaStream_t>(cuda_stream)),
+             "output copy")
+             ? GSPEC_OK
+             : GSPEC_ERR_CUDA;
 }
 
 int gspec_batch_output(gspec_batch* b, int i, void** d_out, uint64_t* bytes, int* complete) {
@@ -227,9 +244,10 @@ int gspec_batch_run(gspec_batch* b, void* cuda_stream) {
       b->err = "a bounded device wait gave up (code " + std::to_string(*h->h_err) + ")";
       return GSPEC_ERR_CUDA;
     }
-  if (!b->exec && !build_graph(b)) return GSPEC_ERR_CUDA;
-  if (!bok(b, cudaGraphLaunch(b->exec, static_cast<cudaStream_t>(cuda_stream)), "graph launch"))
+  if (!b->exec[b->slot] && !build_graph(b, b->slot)) return GSPEC_ERR_CUDA;
+  if (!bok(b, cudaGraphLaunch(b->exec[b->slot], static_cast<cudaStream_t>(cuda_stream)), "graph launch"))
     return GSPEC_ERR_CUDA;
+  b->slot ^= 1;
   ++b->steps;
   return GSPEC_OK;
 }

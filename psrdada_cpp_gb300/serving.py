@@ -66,6 +66,7 @@ def declare(lib) -> None:
     lib.gspec_batch_run.argtypes = [vp, vp]
     lib.gspec_batch_set_input.argtypes = [vp, i32, vp, sz, vp]
     lib.gspec_batch_read_output.argtypes = [vp, i32, vp, sz, vp]
+    lib.gspec_batch_copy_output.argtypes = [vp, i32, vp, sz, vp]
     lib.gspec_batch_kernels_per_step.restype = u64
     lib.gspec_batch_kernels_per_step.argtypes = [vp]
     lib.gspec_batch_steps.restype = u64
@@ -257,6 +258,17 @@ class Batch:
         if rc != GSPEC_OK:
             raise GspecError(self._lib.gspec_batch_last_error(self._b).decode())
         return out
+
+    def copy_output(self, i: int, dst, stream: int = 0) -> None:
+        """Enqueues the copy of member i's accumulator into dst (a pinned torch
+        tensor or (pointer, size)) on ``stream`` without waiting."""
+        if isinstance(dst, tuple):
+            ptr, size = dst
+        else:
+            ptr, size = dst.data_ptr(), dst.numel() * dst.element_size()
+        rc = self._lib.gspec_batch_copy_output(self._b, i, ctypes.c_void_p(ptr), size, ctypes.c_void_p(stream))
+        if rc != GSPEC_OK:
+            raise GspecError(self._lib.gspec_batch_last_error(self._b).decode())
 
     def run(self, stream: int = 0) -> None:
         if self._lib.gspec_batch_run(self._b, ctypes.c_void_p(stream)) != GSPEC_OK:

@@ -241,3 +241,43 @@ def test_autotune_schedules_stay_in_tolerance(tmp_path, stream_blocks):
                 data = [r["data"].tobytes() for r in outs if r["data"] is not None]
             for o, r in zip(data, ref):
                 check_vs_oracle(spec, cfg, o, r)
+
+
+def test_batch_inputs_copied_one_step_ahead(stream_blocks):
+    """The next step's blocks go in on a copy stream while the current step
+    runs (two input buffers per member); results equal the serial loop."""
+    import torch
+    dev = torch.device("cuda", 0)
+    alone = [run_alone_device(spec, blocks) for spec, blocks in stream_blocks]
+    outs = [[] for _ in stream_blocks]
+    compute = torch.cuda.current_stream(dev)
+    copy = torch.cuda.Stream(dev)
+    pinned = [[torch.from_numpy(b).pin_memory() for b in blocks] for _, blocks in stream_blocks]
+    with G.Batch([G.make_config(spec) for spec, _ in stream_blocks]) as bt:
+        copied = [torch.cuda.Event() for _ in range(NBLK)]
+        ran = [torch.cuda.Event() for _ in range(NBLK)]
+
+        def put(k):
+            if k >= 2:
+                copy.wait_event(ran[k - 2])
+            for i in range(bt.n):
+                bt.set_input(i, pinned[i][k], copy.cuda_stream)
+            copied[k].record(copy)
+
+        put(0)
+        for k in range(NBLK):
+            compute.wait_event(copied[k])
+            bt.run(compute.cuda_stream)
+            ran[k].record(compute)
+            if k + 1 < NBLK:
+                put(k + 1)
+            for i in range(bt.n):
+                _, n, complete = bt.output(i)
+                if complete:
+                    dst = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+                    bt.copy_output(i, dst, compute.cuda_stream)
+                    outs[i].append(dst)
+        torch.cuda.synchronize(dev)
+    for i, (spec, _) in enumerate(stream_blocks):
+        got = [o.numpy().tobytes() for o in outs[i]]
+        assert got == alone[i], spec.name
