@@ -258,7 +258,7 @@ def sample_spec(spec, n_out: int):
     return dataclasses.replace(spec, name=spec.name + f"_sample{n_out}", samples_per_pol=per_out * n_out)
 
 
-def cpu_chain_rate(spec, kind: str, seconds: float = 12.0, max_blocks: int = 64):
+def cpu_chain_rate(spec, kind: str, seconds: float = 10.0, max_blocks: int = 1 << 20):
     """Times the C restatement on all host cores; returns (Gsamples/s, cores,
     sample description)."""
     from oracle import gspec_cpu
@@ -723,7 +723,7 @@ def main(argv=None):
                     help="FFT arithmetic: FP32 CUDA cores, or tensor-core DFT-32 stages with BF16/FP16 hi+lo halves")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="wall seconds of the timed CPU sample")
     ap.add_argument("--ref-budget-s", type=float, default=150.0)
     ap.add_argument("--no-tune", action="store_true", help="c4/c5: built-in schedules instead of the autotuner's")
     ap.add_argument("--serve-blocks", type=int, default=10000, help="c5: blocks of the Poisson phase")
