@@ -281,3 +281,28 @@ def test_batch_inputs_copied_one_step_ahead(stream_blocks):
     for i, (spec, _) in enumerate(stream_blocks):
         got = [o.numpy().tobytes() for o in outs[i]]
         assert got == alone[i], spec.name
+
+
+def test_closing_a_waiting_stream_answers_its_blocks(stream_blocks):
+    """A stream closed before it was admitted frees its queue: each queued block
+    comes back with an error status, and the admitted stream is unaffected."""
+    big, small = stream_blocks[1], stream_blocks[0]
+    qb = G.query(G.make_config(big[0], flags=G.FLAG_NO_HOST_BUFFERS)).device_bytes
+    qs = G.query(G.make_config(small[0], flags=G.FLAG_NO_HOST_BUFFERS)).device_bytes
+    with G.Server(max(qb, qs) + min(qb, qs) // 2) as srv:
+        a = srv.open(G.make_config(big[0]))
+        b = srv.open(G.make_config(small[0]))
+        for k, blk in enumerate(small[1][:2]):
+            srv.submit(b, blk, tag=k)
+        assert srv.state(b) == 0
+        srv.close_stream(b)
+        srv.submit(a, big[1][0], tag=7)
+        res = []
+        while len(res) < 3:
+            res += srv.poll(8, 200000)
+        by = {(r["stream"], r["tag"]): r for r in res}
+        assert by[(b, 0)]["status"] < 0 and by[(b, 1)]["status"] < 0
+        assert by[(a, 7)]["status"] == 0
+        assert srv.state(b) == 3
+        with pytest.raises(G.GspecError):
+            srv.submit(b, small[1][0], tag=9)

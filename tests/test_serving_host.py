@@ -101,3 +101,27 @@ def test_entry_points_fail_loudly_without_gpu():
         G.query(G.make_config(synth.config1()))
     with pytest.raises(G.GspecError):
         G.Batch([G.make_config(synth.config1())])
+
+
+def test_poisson_plan_rates_and_order():
+    from psrdada_cpp_gb300 import loadgen
+    specs = [synth.config1()] * 3 + [synth.config3()] * 2
+    rate = 1e9                                            # samples/s per stream
+    plan = loadgen.poisson_plan(specs, rate, 3000, seed=4)
+    assert len(plan) == 3000
+    t = [e[0] for e in plan]
+    assert t == sorted(t) and t[0] >= 0
+    # per-stream block counts follow 1 / block span (config 3 blocks are 32x longer)
+    counts = [sum(1 for _, i in plan if i == k) for k in range(len(specs))]
+    span1 = loadgen.block_samples(synth.config1()) / rate
+    horizon = t[-1]
+    for k in range(3):
+        assert abs(counts[k] - horizon / span1) < 5 * (horizon / span1) ** 0.5
+    assert sum(counts[3:]) < sum(counts[:3]) / 10
+    assert loadgen.poisson_plan(specs, rate, 3000, seed=4) == plan                 # seeded
+
+
+def test_burst_plan_interleaves_streams():
+    from psrdada_cpp_gb300 import loadgen
+    plan = loadgen.burst_plan([synth.config1(), synth.config2()], [3, 2])
+    assert [i for _, i in plan] == [0, 1, 0, 1, 0] and all(t == 0.0 for t, _ in plan)
