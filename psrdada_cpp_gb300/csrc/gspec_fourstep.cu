@@ -144,6 +144,9 @@ __global__ void __launch_bounds__(PassACfg<N1>::THREADS) fourstep_a_kernel(FourS
 #ifndef GSPEC_PASSB_STAGES
 #define GSPEC_PASSB_STAGES 2
 #endif
+#ifndef GSPEC_PASSB_MINB
+#define GSPEC_PASSB_MINB 2   // resident CTAs per SM the register allocation is sized for
+#endif
 
 template <int N2, bool DUAL>
 struct PassBCfg {
@@ -172,7 +175,7 @@ struct PassBCfg {
 // sums in registers over all jobs of the spectrum, adding the jobs in
 // order, so the result does not depend on scheduling.
 template <int N2, bool DUAL>
-__global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, 2) fourstep_b_kernel(FourStepParams p) {
+__global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, GSPEC_PASSB_MINB) fourstep_b_kernel(FourStepParams p) {
   using Cfg = PassBCfg<N2, DUAL>;
   constexpr int J = Cfg::J;
   constexpr int BPT = Cfg::BPT;

@@ -121,8 +121,11 @@ struct SmallCfg {
 // unit's job list (build_jobs) is worked through NSLOT jobs at a time; each
 // slot accumulates its jobs' spectra in shared memory; slots are summed in
 // a fixed order at the end, so results do not depend on scheduling.
+#ifndef GSPEC_SMALL_MINB
+#define GSPEC_SMALL_MINB 2   // resident CTAs per SM the register allocation is sized for
+#endif
 template <int N, int NBITS, bool DUAL>
-__global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS, 2)
+__global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS, GSPEC_SMALL_MINB)
     small_chain_kernel(ChainParams p) {
   using Cfg = SmallCfg<N, DUAL>;
   constexpr int G = Group<NBITS>::samples;
