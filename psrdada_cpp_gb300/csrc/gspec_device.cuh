@@ -345,6 +345,11 @@ __device__ __forceinline__ const uint8_t* pol_byte(const GateParams& g, int pol,
   return g.block + (2ull * h + pol) * g.heap_size + (b32 - h * g.heap_size);
 }
 
+// L2 prefetch of the sector holding p (no register result, no wait).
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // Selected item after the dual-pol merge (edd/src/GatedSpectrometer.cu:9-19:
 // logical OR in the reference convention, bitwise OR in the intended one).
 __device__ __forceinline__ uint64_t load_item(const GateParams& g, uint32_t idx) {

@@ -203,6 +203,24 @@ __global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS, GSPEC_SMALL_MINB)
         for (int e = 0; e < G; ++e) Z[spad(gi * G + e)] = make_float2(re[e], im[e]);
       }
     }
+    {
+      // the next round's samples of this slot into L2 while this round is transformed
+      const uint32_t jn = it + Cfg::NSLOT + slot;
+      if (jn < njobs) {
+        const uint32_t job_n = jobs[jn];
+        const uint32_t fan = job_fa(job_n), fbn = job_fb(job_n);
+#pragma unroll 1
+        for (int gi = t; gi < NG; gi += Cfg::T) {
+          const uint64_t byte0 = static_cast<uint64_t>((f0 + fan) * N + gi * G) * NBITS / 8;
+          prefetch_l2(pol_byte(p.g, 0, byte0));
+          if constexpr (DUAL) {
+            prefetch_l2(pol_byte(p.g, 1, byte0));
+          } else if (fbn != fan && fbn != kNoFrame) {
+            prefetch_l2(pol_byte(p.g, 0, static_cast<uint64_t>((f0 + fbn) * N + gi * G) * NBITS / 8));
+          }
+        }
+      }
+    }
     __syncthreads();
     fft_smem<N, Cfg::P>(Z, twp, t, active);
     if (active) {
