@@ -179,8 +179,8 @@ GateParams gate_params(const gspec_handle* h, const uint8_t* block) {
   return g;
 }
 
-const char* const kKernelNames[kKernelKinds] = {"small_chain", "reduce_finalize", "fourstep_a", "fourstep_b",
-                                                "finalize",    "gate_prepass",    "unused",     "fourstep_plan"};
+const char* const kKernelNames[kKernelKinds] = {"small_chain", "reduce_finalize", "fourstep_a",      "fourstep_b",
+                                                "finalize",    "gate_prepass",    "fourstep_scatter", "fourstep_plan"};
 
 // Launches one kernel of the chain; with profiling on, brackets it with
 // events on its own stream so per-kernel device time can be read back.
@@ -257,6 +257,7 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
     FourStepParams f{};
     f.c = p;
     f.scratch = h->d_scratch;
+    f.bsum = h->d_bsum;
     f.tw1 = h->d_tw1;
     f.tw2 = h->d_tw2;
     f.twA = h->d_twA;
@@ -281,6 +282,8 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
       e = timed(h, 2, s, [&] { return launch_fourstep(N, h->cfg.nbits, h->dual, f, 0, s); });
       if (e != cudaSuccess) return e;
       e = timed(h, 3, s, [&] { return launch_fourstep(N, h->cfg.nbits, h->dual, f, 1, s); });
+      if (e != cudaSuccess) return e;
+      e = timed(h, 6, s, [&] { return launch_fourstep(N, h->cfg.nbits, h->dual, f, 2, s); });
       if (e != cudaSuccess) return e;
     }
   }
@@ -316,7 +319,7 @@ void release(gspec_handle* h) {
   }
   void* ptrs[] = {h->d_sat_dev, h->d_baselines, h->d_pol_stats, h->d_tw,   h->d_tw1,   h->d_tw2,  h->d_twA,
                   h->d_twB,     h->d_partial,   h->d_scratch,   h->d_masks, h->d_flags, h->d_jobs, h->d_njobs,
-                  h->d_dc,      h->d_err,       h->d_tc_hi,     h->d_tc_lo, h->d_tc_w, h->d_tc_img};
+                  h->d_dc,      h->d_err,       h->d_tc_hi,     h->d_tc_lo, h->d_tc_w, h->d_tc_img, h->d_bsum};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->h_err) cudaFreeHost(h->h_err);
@@ -454,6 +457,11 @@ bool plan_handle(gspec_handle* h) {
   return true;
 }
 
+// Pass-B row-pair sums of one chunk of output spectra (four-step path).
+uint64_t bsum_bytes(const gspec_handle* h) {
+  return static_cast<uint64_t>(h->kchunk) * (h->N1 / 2) * (h->dual ? 8 : 2) * (h->N2 + 1) * sizeof(float);
+}
+
 // Device bytes gspec_create allocates for a planned handle (the same list
 // and the same 16-byte minimum as its dalloc calls).
 uint64_t footprint(const gspec_handle* h) {
@@ -472,6 +480,7 @@ uint64_t footprint(const gspec_handle* h) {
     t += sz(static_cast<uint64_t>(h->kchunk) * h->maxjobs * N * sizeof(float2));
     t += sz(h->n_out * h->maxjobs * sizeof(uint32_t)) + sz(h->n_out * sizeof(uint32_t)) +
          sz(2ull * h->n_out * sizeof(uint32_t));
+    t += sz(bsum_bytes(h));
     if (h->cfg.form != GSPEC_FORM_FP32)
       t += 2 * sz(4096 * sizeof(uint16_t)) + sz(1024 * sizeof(float2)) + sz(tc::kImageBytesHost);
   }
@@ -589,7 +598,8 @@ gspec_handle* gspec_create(const gspec_config* cfg, char* err, size_t err_len) {
     if (!dalloc(h, &h->d_scratch, slots * static_cast<uint64_t>(N) * sizeof(float2), "four-step scratch") ||
         !dalloc(h, &h->d_jobs, h->n_out * h->maxjobs * sizeof(uint32_t), "job lists") ||
         !dalloc(h, &h->d_njobs, h->n_out * sizeof(uint32_t), "job counts") ||
-        !dalloc(h, &h->d_dc, 2ull * h->n_out * sizeof(uint32_t), "dc counts"))
+        !dalloc(h, &h->d_dc, 2ull * h->n_out * sizeof(uint32_t), "dc counts") ||
+        !dalloc(h, &h->d_bsum, gspec_engine::bsum_bytes(h), "pass-B sums"))
       return bail("");
     if (cfg->form != GSPEC_FORM_FP32) {
       if (!dalloc(h, &h->d_tc_hi, 4096 * sizeof(uint16_t), "tensor-core operand") ||

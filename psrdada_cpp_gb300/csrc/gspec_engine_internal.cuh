@@ -52,6 +52,7 @@ struct gspec_handle {
   uint16_t* d_tc_lo = nullptr;
   float2* d_tc_w = nullptr;        // W1024 twiddles
   uint8_t* d_tc_img = nullptr;     // [B_hi | B_lo | W1024] in shared-memory layout
+  float* d_bsum = nullptr;         // pass-B row-pair sums of one chunk
   uint32_t maxjobs = 0;
   int32_t heap_shift = -1;
   uint32_t* d_err = nullptr;       // set by kernels whose bounded waits gave up
@@ -86,6 +87,7 @@ bool plan_units(gspec_handle* h);
 bool plan_handle(gspec_handle* h);
 // Device bytes gspec_create allocates for a planned handle.
 uint64_t footprint(const gspec_handle* h);
+uint64_t bsum_bytes(const gspec_handle* h);
 void fill_info(const gspec_handle* h, gspec_info* info);
 // Enqueues the whole chain for one block on stream s using h's buffers.
 cudaError_t run_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out, unsigned long long* d_sat,

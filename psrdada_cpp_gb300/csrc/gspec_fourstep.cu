@@ -324,20 +324,51 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, GSPEC_PASSB_MINB)
       }
     }
   }
-  float* outf = reinterpret_cast<float*>(p.c.out + k * p.c.out_rec);
+  // row-pair sums, contiguous in the slot a (coalesced); fourstep_scatter_kernel
+  // adds them into the output bins, whose index c strides by N1 along a
+  float* bs = p.bsum + static_cast<size_t>(blockIdx.x) * VALS * (N2 + 1);
+  (void)C;
 #pragma unroll
   for (int i = 0; i < BPT; ++i) {
     const int a = tid + i * Cfg::THREADS;
     if (a >= nbins) continue;
-    uint32_t c;
-    if (rp != 0) {
-      c = a < N2 / 2 ? rp + N1 * a : (N1 - rp) + N1 * (a - N2 / 2);
-    } else {
-      c = a <= N2 / 2 ? N1 * a : half + N1 * (a - N2 / 2 - 1);
-    }
 #pragma unroll
-    for (int v = 0; v < VALS; ++v) outf[static_cast<size_t>(v) * C + c] += acc[i][v];
+    for (int v = 0; v < VALS; ++v) bs[v * (N2 + 1) + a] = acc[i][v];
   }
+}
+
+// Adds the row-pair sums of one launch into the output spectra: thread per
+// output bin c (coalesced read-modify-write of the output record), reading
+// the slot a of row pair rp that holds c (the inverse of pair_slot):
+//   k1 = c % N1, k2 = c / N1; k1 = 0: rp 0, a = k2; k1 = N1/2: rp 0,
+//   a = N2/2 + 1 + k2; k1 < N1/2: rp = k1, a = k2; else rp = N1 - k1,
+//   a = N2/2 + k2.
+// grid = (ceil(C / 256), nk * VALS).
+__global__ void fourstep_scatter_kernel(FourStepParams p, int vals) {
+  const uint32_t N1 = p.N1, N2 = p.N2;
+  const uint32_t C = N1 * N2 / 2 + 1;
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  const uint32_t kk = blockIdx.y / vals;
+  const uint32_t v = blockIdx.y - kk * vals;
+  const uint32_t k1 = c % N1, k2 = c / N1;
+  uint32_t rp, a;
+  if (k1 == 0) {
+    rp = 0;
+    a = k2;
+  } else if (k1 == N1 / 2) {
+    rp = 0;
+    a = N2 / 2 + 1 + k2;
+  } else if (k1 < N1 / 2) {
+    rp = k1;
+    a = k2;
+  } else {
+    rp = N1 - k1;
+    a = N2 / 2 + k2;
+  }
+  const float add = p.bsum[((static_cast<size_t>(kk) * (N1 / 2) + rp) * vals + v) * (N2 + 1) + a];
+  float* outf = reinterpret_cast<float*>(p.c.out + (p.k0 + kk) * p.c.out_rec);
+  outf[static_cast<size_t>(v) * C + c] += add;
 }
 
 // ------------------------------------------------------------ dispatch
@@ -407,11 +438,17 @@ static cudaError_t launch_fs(int nbits, const FourStepParams& p, int pass, cudaS
   return cudaErrorInvalidValue;
 }
 
-// pass: -1 plan, 0 pass A, 1 pass B
+// pass: -1 plan, 0 pass A, 1 pass B, 2 scatter of the pass-B sums
 cudaError_t launch_fourstep(int N, int nbits, bool dual, const FourStepParams& p, int pass, cudaStream_t s) {
   (void)N;
   if (pass < 0) {
     fourstep_plan_kernel<<<(p.nk + 63) / 64, 64, 0, s>>>(p, dual ? 1 : 0);
+    return cudaGetLastError();
+  }
+  if (pass == 2) {
+    const int vals = dual ? 8 : 2;
+    const uint32_t C = p.N1 * p.N2 / 2 + 1;
+    fourstep_scatter_kernel<<<dim3((C + 255) / 256, p.nk * vals), 256, 0, s>>>(p, vals);
     return cudaGetLastError();
   }
   if (p.form != 0 && ((pass == 0 && p.N1 == 1024) || (pass == 1 && p.N2 == 1024)))

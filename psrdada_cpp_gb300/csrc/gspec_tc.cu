@@ -489,19 +489,15 @@ __global__ void __launch_bounds__(kPassThreads, 2) tc_b_kernel(FourStepParams p)
       }
     }
   }
-  float* outf = reinterpret_cast<float*>(p.c.out + k * p.c.out_rec);
+  // row-pair sums, contiguous in the slot a; the scatter kernel adds them to the output
+  float* bs = p.bsum + static_cast<size_t>(blockIdx.x) * VALS * (N2 + 1);
+  (void)C;
 #pragma unroll
   for (int i = 0; i < BPT; ++i) {
     const int a = tid + i * kPassThreads;
     if (a >= nbins) continue;
-    uint32_t c;
-    if (rp != 0) {
-      c = a < N2 / 2 ? rp + N1 * a : (N1 - rp) + N1 * (a - N2 / 2);
-    } else {
-      c = a <= N2 / 2 ? N1 * a : half + N1 * (a - N2 / 2 - 1);
-    }
 #pragma unroll
-    for (int v = 0; v < VALS; ++v) outf[static_cast<size_t>(v) * C + c] += acc[i][v];
+    for (int v = 0; v < VALS; ++v) bs[v * (N2 + 1) + a] = acc[i][v];
   }
   fence_after();
   if (tid < 32) tmem_dealloc(s.tmem, kTmemCols);
