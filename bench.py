@@ -628,7 +628,7 @@ def run_serve(args):
     m = args.serve_peak_blocks
     burst = loadgen.burst_plan(specs, [m * ratio] * 16 + [m] * 16)
     prios = {} if args.no_priority else loadgen.span_priorities(specs)
-    infl = int(args.inflight_gb * 2**30)
+    infl = args.inflight_long * host[c3.name][0].numel()
     peak = loadgen.run(specs, host, burst, budget, device=local, tunes=tunes, priorities=prios, inflight_bytes=infl)
     rate = 0.6 * peak["gsamples_per_s"] * 1e9 / len(specs)
     plan = loadgen.poisson_plan(specs, rate, args.serve_blocks, seed=4)
@@ -730,7 +730,8 @@ def main(argv=None):
     ap.add_argument("--serve-peak-blocks", type=int, default=4, help="c5: fft-2^20 blocks per stream, peak phase")
     ap.add_argument("--budget-gb", type=float, default=120.0, help="c5: device memory budget of the server")
     ap.add_argument("--no-priority", action="store_true", help="c5: equal CUDA stream priorities")
-    ap.add_argument("--inflight-gb", type=float, default=0.0, help="c5: input bytes on the GPU at once (0: no limit)")
+    ap.add_argument("--inflight-long", type=int, default=0,
+                    help="c5: fft-2^20 blocks on the GPU at once over all streams (0: no limit)")
     ap.add_argument("--connections", type=int, default=32, help="c5: CUDA_DEVICE_MAX_CONNECTIONS")
     args = ap.parse_args(argv)
     if args.warmup < 3:

@@ -214,9 +214,10 @@ typedef struct gspec_server_config {
   int32_t max_inflight;     /* blocks of one stream on the GPU at once (1 or 2; 0 = 2) */
   int32_t output_buffers;   /* pinned host output buffers per stream (0 = 2) */
   int32_t reserved;
-  uint64_t inflight_bytes;  /* input bytes of all streams' blocks on the GPU at once (0 = no limit); a
-                               block that would exceed it waits unless nothing is in flight.  Bounds
-                               the copy and kernel queues that short blocks wait behind */
+  uint64_t inflight_bytes;  /* input bytes of all streams' long blocks (> 64 MiB) on the GPU at once
+                               (0 = no limit); a long block that would exceed it waits unless no long
+                               block is in flight, short blocks never wait for it.  Bounds the copy
+                               and kernel queues that short blocks wait behind */
 } gspec_server_config;
 typedef struct gspec_result {
   int32_t stream;           /* stream id */
@@ -234,6 +235,10 @@ typedef struct gspec_result {
    * the wait between copy and chain (earlier blocks of the stream, the
    * output accumulator), the chain's kernels, and the output copy. */
   float h2d_ms, wait_ms, chain_ms, d2h_ms;
+  /* From the block's first copy issued (t_start) to the GPU starting that
+   * copy, and from the GPU finishing the block to t_done, in ms (the GPU
+   * clock mapped onto the server clock by an event at server creation). */
+  float issue_ms, observe_ms;
 } gspec_result;
 gspec_server* gspec_server_create(const gspec_server_config* cfg, char* err, size_t err_len);
 /* Waits for the streams' outstanding blocks, then frees everything. */
@@ -246,7 +251,8 @@ int gspec_stream_open(gspec_server* s, const gspec_config* cfg, int* stream_id);
 int gspec_stream_state(gspec_server* s, int stream_id);
 /* Queues one block.  The host memory must stay valid and unchanged until
  * the block's result has been returned by gspec_poll; page-locked memory
- * lets its copy overlap the GPU work of other blocks. */
+ * lets its copy overlap the GPU work of other blocks, and a page-locked
+ * block of at most 64 MiB is read by SM loads instead of a copy engine. */
 int gspec_submit(gspec_server* s, int stream_id, const void* block, size_t size, uint64_t tag);
 /* Returns up to max finished results (oldest first), waiting up to
  * timeout_us microseconds for the first one. */

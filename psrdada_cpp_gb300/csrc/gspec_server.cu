@@ -11,7 +11,8 @@
 //     output accumulators, twiddles, scratch) resident in device memory;
 //   * continuous batching: a stream's next block is issued as soon as it is
 //     queued, its stream has fewer than max_inflight blocks on the GPU, the
-//     input bytes on the GPU stay within inflight_bytes and a host output
+//     input bytes of long blocks (> 64 MiB) on the GPU stay within
+//     inflight_bytes (short blocks are never held back) and a host output
 //     buffer is free, so blocks of different streams overlap on the device in
 //     their own CUDA streams (streams are scanned in id order each pass);
 //   * completion: each block's last operation records an event; the loop
@@ -55,7 +56,7 @@ struct Flight {
   double t_start;
   int obuf;        // host output buffer, -1 when the block completes no output
   cudaEvent_t done;
-  uint64_t bytes;  // input bytes (in-flight limit)
+  uint64_t bytes;  // input bytes of a long block (in-flight limit), else 0
   int slot;        // event slot of the stage timings
 };
 
@@ -96,8 +97,10 @@ struct gspec_server {
   std::deque<int> admit;
   std::deque<gspec_result> results;
   uint64_t in_use = 0;
-  uint64_t inflight_bytes = 0;  // input bytes of the blocks on the GPU
+  uint64_t inflight_bytes = 0;  // input bytes of the long blocks on the GPU
   uint64_t launches_done = 0;   // launches of streams already closed
+  cudaEvent_t epoch = nullptr;  // GPU time of server-clock second t_epoch
+  double t_epoch = 0;
   bool stop = false;
   std::thread worker;
   std::string err;
@@ -193,7 +196,10 @@ bool admit_stream(const gspec_server_config& scfg, const gspec_config& cfg, int 
 // Large copies go out in pieces: the copy engines take work from the streams
 // of all served streams piece by piece, so a short block's copy waits for at
 // most one piece of a long block's copy instead of the whole of it.
-constexpr size_t kCopyPiece = 8u << 20;
+#ifndef GSPEC_COPY_PIECE_MB
+#define GSPEC_COPY_PIECE_MB 8
+#endif
+constexpr size_t kCopyPiece = static_cast<size_t>(GSPEC_COPY_PIECE_MB) << 20;
 
 cudaError_t copy_pieces(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t s) {
   auto* d = static_cast<char*>(dst);
@@ -206,9 +212,25 @@ cudaError_t copy_pieces(void* dst, const void* src, size_t bytes, cudaMemcpyKind
   return cudaSuccess;
 }
 
-// Outputs up to this size reach the host by SM stores on the compute stream
-// (no copy engine: they never queue behind other streams' bulk copies).
+// Short blocks (inputs up to kShortBlockMax) and outputs up to kStoreCopyMax
+// move between page-locked host memory and the GPU by SM loads and stores on
+// the compute stream: the copy engines take copies in the order they were
+// issued, so a short block's copy would otherwise wait behind every long
+// block's copy issued before it.  Short blocks are never held back by the
+// server's in-flight limit either.
+constexpr uint64_t kShortBlockMax = 64u << 20;
 constexpr uint64_t kStoreCopyMax = 16u << 20;
+
+// Device address of a page-locked host block, or nullptr (pageable memory,
+// device memory) when the block goes through the copy engines.
+const void* mapped_host(const void* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
 
 // Enqueues one block of an admitted stream on its handle's streams.
 bool issue(gspec_server* s, Stream& st, const Queued& q, int obuf) {
@@ -219,15 +241,24 @@ bool issue(gspec_server* s, Stream& st, const Queued& q, int obuf) {
   const bool first = q.index % nb == 0;
   const bool last = obuf >= 0;
   const int es = st.ev_next;
-  Flight f{q.index, q.tag, q.t_submit, now_s(s), obuf, st.ev[es], q.size, es};
+  Flight f{q.index, q.tag, q.t_submit, now_s(s), obuf, st.ev[es], q.size > kShortBlockMax ? q.size : 0, es};
   st.ev_next = (st.ev_next + 1) % kEventsPerStream;
-  if (!ok(st, cudaStreamWaitEvent(h->h2d, h->ev_in_free[slot], 0), "wait input") ||
-      !ok(st, cudaEventRecord(st.ev_stage[0][es], h->h2d), "record") ||
-      !ok(st, copy_pieces(h->d_in[slot], q.data, q.size, cudaMemcpyDefault, h->h2d), "H2D block") ||
-      !ok(st, cudaEventRecord(h->ev_h2d[slot], h->h2d), "record") ||
-      !ok(st, cudaEventRecord(st.ev_stage[1][es], h->h2d), "record") ||
-      !ok(st, cudaStreamWaitEvent(h->proc, h->ev_h2d[slot], 0), "wait H2D"))
+  const void* src_dev = q.size <= kShortBlockMax && q.size % 8 == 0 ? mapped_host(q.data) : nullptr;
+  if (src_dev) {
+    // the compute stream's earlier chains are the input slot's only readers
+    if (!ok(st, cudaEventRecord(st.ev_stage[0][es], h->proc), "record") ||
+        !ok(st, gspec::launch_copy_words(h->d_in[slot], src_dev, q.size, h->sm_count, h->proc), "input copy") ||
+        !ok(st, cudaEventRecord(st.ev_stage[1][es], h->proc), "record"))
+      return false;
+    h->launches += 1;
+  } else if (!ok(st, cudaStreamWaitEvent(h->h2d, h->ev_in_free[slot], 0), "wait input") ||
+             !ok(st, cudaEventRecord(st.ev_stage[0][es], h->h2d), "record") ||
+             !ok(st, copy_pieces(h->d_in[slot], q.data, q.size, cudaMemcpyDefault, h->h2d), "H2D block") ||
+             !ok(st, cudaEventRecord(h->ev_h2d[slot], h->h2d), "record") ||
+             !ok(st, cudaEventRecord(st.ev_stage[1][es], h->h2d), "record") ||
+             !ok(st, cudaStreamWaitEvent(h->proc, h->ev_h2d[slot], 0), "wait H2D")) {
     return false;
+  }
   if (first) {
     // the accumulator's previous D2H must be done before it is cleared
     if (!ok(st, cudaStreamWaitEvent(h->proc, st.ev_out_done[oi], 0), "wait D2H") ||
@@ -271,7 +302,7 @@ bool issue(gspec_server* s, Stream& st, const Queued& q, int obuf) {
   return true;
 }
 
-gspec_result make_result(const Stream& st, const Flight& f, int status, double t_done) {
+gspec_result make_result(const gspec_server* s, const Stream& st, const Flight& f, int status, double t_done) {
   gspec_result r{};
   r.stream = st.id;
   r.status = status;
@@ -292,6 +323,11 @@ gspec_result make_result(const Stream& st, const Flight& f, int status, double t
     r.wait_ms = ms(st.ev_stage[1][f.slot], st.ev_stage[2][f.slot]);
     r.chain_ms = ms(st.ev_stage[2][f.slot], st.ev_stage[3][f.slot]);
     r.d2h_ms = ms(st.ev_stage[3][f.slot], f.done);
+    if (s->epoch) {
+      const float g0 = ms(s->epoch, st.ev_stage[0][f.slot]), g1 = ms(s->epoch, f.done);
+      if (g0 >= 0.f) r.issue_ms = static_cast<float>((s->t_epoch + g0 * 1e-3 - f.t_start) * 1e3);
+      if (g1 >= 0.f) r.observe_ms = static_cast<float>((t_done - s->t_epoch - g1 * 1e-3) * 1e3);
+    }
   }
   return r;
 }
@@ -335,43 +371,53 @@ void worker_loop(gspec_server* s) {
       lk.lock();
     }
     bool busy = false;
+    // completions of every stream, in order per stream: runs before the issue
+    // pass and again after every issued block, so a long block's issue (many
+    // copy pieces and launches) delays no other stream's result
+    auto complete_all = [&]() {
+      for (size_t kc = 0; kc < s->streams.size(); ++kc) {
+        Stream& st = *s->streams[kc];
+        if (st.state != 1 && st.state != 2) continue;
+        while (!st.flight.empty()) {
+          Flight& f = st.flight.front();
+          const cudaError_t q = cudaEventQuery(f.done);
+          if (q == cudaErrorNotReady) break;
+          int status = GSPEC_OK;
+          if (q != cudaSuccess) {
+            status = GSPEC_ERR_CUDA;
+            st.h->err = std::string("block failed: ") + cudaGetErrorString(q);
+            st.failed = true;
+          } else if (st.h->h_err && *st.h->h_err) {
+            status = GSPEC_ERR_CUDA;
+            st.h->err = "a bounded device wait gave up (code " + std::to_string(*st.h->h_err) + ")";
+            st.failed = true;
+          }
+          s->results.push_back(make_result(s, st, f, status, now_s(s)));
+          s->inflight_bytes -= f.bytes;
+          st.flight.pop_front();
+          progress = true;
+          s->cv_result.notify_all();
+        }
+      }
+    };
+    complete_all();
     for (size_t k = 0; k < s->streams.size(); ++k) {
       Stream& st = *s->streams[k];
       if (st.state != 1 && st.state != 2) continue;
-      // completions, in order
-      while (!st.flight.empty()) {
-        Flight& f = st.flight.front();
-        const cudaError_t q = cudaEventQuery(f.done);
-        if (q == cudaErrorNotReady) break;
-        int status = GSPEC_OK;
-        if (q != cudaSuccess) {
-          status = GSPEC_ERR_CUDA;
-          st.h->err = std::string("block failed: ") + cudaGetErrorString(q);
-          st.failed = true;
-        } else if (st.h->h_err && *st.h->h_err) {
-          status = GSPEC_ERR_CUDA;
-          st.h->err = "a bounded device wait gave up (code " + std::to_string(*st.h->h_err) + ")";
-          st.failed = true;
-        }
-        s->results.push_back(make_result(st, f, status, now_s(s)));
-        s->inflight_bytes -= f.bytes;
-        st.flight.pop_front();
-        progress = true;
-        s->cv_result.notify_all();
-      }
       // issue
       while (!st.queue.empty() && static_cast<int>(st.flight.size()) < max_inflight) {
         const Queued& q = st.queue.front();
         if (st.failed || !st.h) {
           Flight f{q.index, q.tag, q.t_submit, now_s(s), -1, nullptr, 0, -1};
-          s->results.push_back(make_result(st, f, GSPEC_ERR_STATE, now_s(s)));
+          s->results.push_back(make_result(s, st, f, GSPEC_ERR_STATE, now_s(s)));
           st.queue.pop_front();
           s->cv_result.notify_all();
           progress = true;
           continue;
         }
-        if (s->cfg.inflight_bytes && s->inflight_bytes > 0 && s->inflight_bytes + q.size > s->cfg.inflight_bytes)
-          break;   // the GPU holds enough work: wait for a block to finish
+        if (q.size > kShortBlockMax && s->cfg.inflight_bytes && s->inflight_bytes > 0 &&
+            s->inflight_bytes + q.size > s->cfg.inflight_bytes)
+          break;   // the GPU holds enough long blocks: wait for one to finish
         int obuf = -1;
         if ((q.index + 1) % st.info.n_blocks == 0) {
           for (size_t i = 0; i < st.hfree.size(); ++i)
@@ -388,6 +434,7 @@ void worker_loop(gspec_server* s) {
         }
         st.queue.pop_front();
         progress = true;
+        complete_all();
       }
       if (!st.flight.empty()) busy = true;
       if (st.state == 2 && stream_idle(st)) {
@@ -447,6 +494,19 @@ gspec_server* gspec_server_create(const gspec_server_config* cfg, char* err, siz
   auto* s = new gspec_server();
   s->cfg = *cfg;
   s->t0 = Clock::now();
+  // the GPU clock against the server clock: an event on an idle stream,
+  // recorded after the host time is taken
+  cudaStream_t es = nullptr;
+  if (cudaStreamCreateWithFlags(&es, cudaStreamNonBlocking) == cudaSuccess) {
+    if (cudaEventCreate(&s->epoch) == cudaSuccess) {
+      s->t_epoch = now_s(s);
+      if (cudaEventRecord(s->epoch, es) != cudaSuccess || cudaEventSynchronize(s->epoch) != cudaSuccess) {
+        cudaEventDestroy(s->epoch);
+        s->epoch = nullptr;
+      }
+    }
+    cudaStreamDestroy(es);
+  }
   s->worker = std::thread(worker_loop, s);
   return s;
 }
@@ -461,6 +521,7 @@ void gspec_server_destroy(gspec_server* s) {
   s->worker.join();
   cudaSetDevice(s->cfg.device);
   for (auto& up : s->streams) free_stream_memory(*up);
+  if (s->epoch) cudaEventDestroy(s->epoch);
   delete s;
 }
 

@@ -105,7 +105,8 @@ def run(specs: list, host_blocks: dict, plan: list, memory_budget: int, device: 
                         srv.release(r["stream"], r["buffer"])     # the spectrum is not kept
                     i = sid_index[r["stream"]]
                     records.append((i, r["block_index"], r["t_submit"], r["t_start"], r["t_done"], r["status"],
-                                    r["data"] is not None, r["h2d_ms"], r["wait_ms"], r["chain_ms"], r["d2h_ms"]))
+                                    r["data"] is not None, r["h2d_ms"], r["wait_ms"], r["chain_ms"], r["d2h_ms"],
+                                    r["issue_ms"], r["observe_ms"]))
                     if r["status"] != 0:
                         err.append(srv.last_error())
                     if keep_outputs and r["data"] is not None:
@@ -132,7 +133,7 @@ def run(specs: list, host_blocks: dict, plan: list, memory_budget: int, device: 
         srv.close()
     if err:
         raise RuntimeError(f"serving errors: {err[:3]}")
-    rec = np.array([(r[0], r[1], r[2], r[3], r[4], r[7], r[8], r[9], r[10]) for r in records])
+    rec = np.array([(r[0], r[1], r[2], r[3], r[4], r[7], r[8], r[9], r[10], r[11], r[12]) for r in records])
     samples = sum(block_samples(specs[int(i)]) for i in rec[:, 0])
     return {"records": rec, "elapsed_s": t1 - t0, "samples": samples,
             "gsamples_per_s": samples / (t1 - t0) / 1e9, "launches": launches, "outputs": outputs}
@@ -157,7 +158,7 @@ def latency_summary(res: dict, specs: list, rate_per_stream: float | None = None
              "p99_ms": float(np.percentile(l, 99)),
              "queue_p50_ms": float(np.percentile(q, 50)), "queue_p99_ms": float(np.percentile(q, 99)),
              "gpu_p50_ms": float(np.percentile(g, 50)), "gpu_p99_ms": float(np.percentile(g, 99))}
-        for k, name_ in ((5, "h2d"), (6, "wait"), (7, "chain"), (8, "d2h")):
+        for k, name_ in ((5, "h2d"), (6, "wait"), (7, "chain"), (8, "d2h"), (9, "issue"), (10, "observe")):
             v = rec[sel, k]
             d[f"{name_}_p50_ms"] = float(np.percentile(v, 50))
             d[f"{name_}_p99_ms"] = float(np.percentile(v, 99))

@@ -29,7 +29,8 @@ class GspecResult(ctypes.Structure):
                 ("block_index", ctypes.c_uint64), ("data", ctypes.c_void_p), ("size", ctypes.c_uint64),
                 ("buffer", ctypes.c_int32), ("reserved", ctypes.c_int32), ("t_submit", ctypes.c_double),
                 ("t_start", ctypes.c_double), ("t_done", ctypes.c_double), ("h2d_ms", ctypes.c_float),
-                ("wait_ms", ctypes.c_float), ("chain_ms", ctypes.c_float), ("d2h_ms", ctypes.c_float)]
+                ("wait_ms", ctypes.c_float), ("chain_ms", ctypes.c_float), ("d2h_ms", ctypes.c_float),
+                ("issue_ms", ctypes.c_float), ("observe_ms", ctypes.c_float)]
 
 
 def declare(lib) -> None:
@@ -166,6 +167,7 @@ class Server:
             d = {"stream": r.stream, "status": r.status, "tag": r.tag, "block_index": r.block_index,
                  "t_submit": r.t_submit, "t_start": r.t_start, "t_done": r.t_done, "buffer": r.buffer,
                  "h2d_ms": r.h2d_ms, "wait_ms": r.wait_ms, "chain_ms": r.chain_ms, "d2h_ms": r.d2h_ms,
+                 "issue_ms": r.issue_ms, "observe_ms": r.observe_ms,
                  "size": r.size, "data": None}
             if r.data and copy:
                 d["data"] = np.ctypeslib.as_array((ctypes.c_uint8 * r.size).from_address(r.data)).copy()

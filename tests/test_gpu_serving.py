@@ -66,10 +66,15 @@ def check_vs_oracle(spec, cfg, got: bytes, ref):
     assert err <= SPEC_TOL, (spec.name, err)
 
 
-def serve(streams_blocks, budget=64 << 30, order="interleaved"):
-    """Runs the streams through one Server; returns {stream index: [output bytes]}."""
+def serve(streams_blocks, budget=64 << 30, order="interleaved", pinned=False, **server_args):
+    """Runs the streams through one Server; returns {stream index: [output bytes]}.
+    ``pinned`` submits page-locked copies of the blocks (read by SM loads)."""
+    if pinned:
+        import torch
+        streams_blocks = [(spec, [torch.from_numpy(b).pin_memory() for b in blocks])
+                          for spec, blocks in streams_blocks]
     outs = {i: [] for i in range(len(streams_blocks))}
-    with G.Server(budget) as srv:
+    with G.Server(budget, **server_args) as srv:
         ids = [srv.open(G.make_config(spec)) for spec, _ in streams_blocks]
         jobs = []
         for i, (_, blocks) in enumerate(streams_blocks):
@@ -122,6 +127,23 @@ def test_serving_alone_equals_mix(stream_blocks):
         for a, m, r in zip(alone[i], mix[i], ref):
             assert a == m, f"{spec.name}: result differs between alone and mix"
             check_vs_oracle(spec, cfg, a, r)
+
+
+def test_serving_pinned_inputs_equal_pageable(stream_blocks):
+    """Page-locked blocks (SM loads on the compute stream) give the same bytes
+    as pageable blocks (copy engine on the copy stream)."""
+    assert serve(stream_blocks, pinned=True) == serve(stream_blocks)
+
+
+def test_serving_inflight_cap_equals_default(stream_blocks):
+    """A cap on the long blocks in flight gives the same bytes as the
+    default server."""
+    big = S("g_d12_n65536_long", 12, True, 6144, 1, 1 << 25, 1 << 16, 4, diode_period_heaps=5)
+    blocks = [synth.make_block(big, seed=60 + b, block_index=b) for b in range(2)]
+    assert blocks[0].nbytes > 64 << 20
+    mix = [(big, blocks), (big, blocks[::-1])] + stream_blocks[:2]
+    ref = serve(mix)
+    assert serve(mix, inflight_bytes=blocks[0].nbytes) == ref
 
 
 def test_serving_admission_by_budget(stream_blocks):

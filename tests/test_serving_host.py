@@ -23,7 +23,8 @@ STRUCTS = {
     "gspec_server_config": (serving.GspecServerConfig, ["memory_budget", "device", "max_inflight",
                                                         "output_buffers", "inflight_bytes"]),
     "gspec_result": (serving.GspecResult, ["stream", "status", "tag", "block_index", "data", "size", "buffer",
-                                           "t_submit", "t_start", "t_done", "h2d_ms", "wait_ms", "chain_ms", "d2h_ms"]),
+                                           "t_submit", "t_start", "t_done", "h2d_ms", "wait_ms", "chain_ms", "d2h_ms",
+                                           "issue_ms", "observe_ms"]),
 }
 
 
