@@ -236,10 +236,14 @@ def tensor_roofline(spec, info, form, kernels, nprof, G):
     ms = sum(kernels[k][2] for k in ("fourstep_a", "fourstep_b") if k in kernels
              and ((k == "fourstep_a" and n1 == 1024) or (k == "fourstep_b" and n2 == 1024))) / nprof
     ach = flops / (ms / 1e3) / 1e12 if ms > 0 else None
+    _, _, peaks = measured_peaks()
+    if "bf16_tflops" in peaks:
+        peak, source = float(peaks["bf16_tflops"]), "measured dense bf16 (cuBLAS burst)"
+    else:
+        peak, source = FALLBACK_BF16_TFLOPS, "fallback dense bf16 (no measured peak file)"
     return {"bound": "tensor", "mma_flops_per_block": flops, "dft1024_per_block": transforms,
             "tensor_pass_ms_per_block": round(ms, 4), "achieved_tflops": round(ach, 2) if ach else None,
-            "peak_tflops": FALLBACK_BF16_TFLOPS, "peak_source": "fallback dense bf16 (no measured peak file)",
-            "frac": round(ach / FALLBACK_BF16_TFLOPS, 5) if ach else None}
+            "peak_tflops": peak, "peak_source": source, "frac": round(ach / peak, 5) if ach else None}
 
 
 def cpu_cores() -> int:
