@@ -34,6 +34,7 @@ then Poisson arrivals at 60 % of that rate, with block-to-spectrum latency.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import math
 import os
@@ -407,8 +408,9 @@ def run_gpu(args):
         for i in range(max(3, args.warmup)):
             ge(raws[i % 2])
         torch.cuda.synchronize(dev)
-        ke = max(8, min(args.steps, 400))
+        ke = max(8, min(args.steps, 1000))
         dist_barrier()
+        gc.disable()     # as timeit does: no collector pauses inside the timed loop
         t0 = time.perf_counter()
         for i in range(ke):
             c0 = time.perf_counter()
@@ -416,6 +418,7 @@ def run_gpu(args):
             lat.append((time.perf_counter() - c0) * 1e3)
         torch.cuda.synchronize(dev)
         t1 = time.perf_counter()
+        gc.enable()
         dist_barrier()
         e_s = dist_max(t1 - t0, dev)
         e_val = dist_sum(samples_per_step * ke, dev) / e_s / 1e9

@@ -34,6 +34,7 @@ struct gspec_handle {
   unsigned long long* d_sat[2] = {nullptr, nullptr};
   unsigned long long* d_sat_dev = nullptr;
   char* h_out[2] = {nullptr, nullptr};
+  char* h_out_dev[2] = {nullptr, nullptr};   // their device addresses (SM-store output copies)
   float* d_baselines = nullptr;
   unsigned long long* d_pol_stats = nullptr;
   float2* d_tw = nullptr;

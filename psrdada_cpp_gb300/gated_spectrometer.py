@@ -250,11 +250,13 @@ class GatedSpectrometer:
         self._h = ctypes.c_void_p(h)
         self._handler = handler
         self._out = GspecOutput()
+        self._views = {}
         self.config = cfg
         self.layout = layout
 
     # -- lifetime
     def close(self):
+        self._views = {}
         if getattr(self, "_h", None):
             self._lib.gspec_destroy(self._h)
             self._h = None
@@ -296,7 +298,11 @@ class GatedSpectrometer:
             return True
         if self._out.ready:
             n = self._out.size
-            view = np.ctypeslib.as_array((ctypes.c_uint8 * n).from_address(self._out.data))
+            key = (self._out.data, n)
+            view = self._views.get(key)
+            if view is None:   # one view per pinned output buffer, made once
+                view = np.ctypeslib.as_array((ctypes.c_uint8 * n).from_address(self._out.data))
+                self._views[key] = view
             self._handler(RawBytes(view, n, n))
         return False
 
