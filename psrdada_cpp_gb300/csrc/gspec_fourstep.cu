@@ -81,6 +81,8 @@ __global__ void __launch_bounds__(PassACfg<N1>::THREADS) fourstep_a_kernel(FourS
   const bool count_stats = (c0 == gbase || G <= BC);
   const uint32_t sg_a = count_stats ? (DUAL ? (1u << ga) : 3u) : 0u;
 
+  static_assert((N1 * GPR + Cfg::THREADS - 1) / Cfg::THREADS * G <= 128 && Cfg::THREADS <= 512,
+                "per-thread gate statistics fit the 32-bit commit");
   GateStats st[NPOL];
   for (int w = tid; w < N1 * GPR; w += Cfg::THREADS) {
     const int n1 = w % N1;

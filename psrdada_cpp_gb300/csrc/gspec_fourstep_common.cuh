@@ -6,55 +6,55 @@
 
 namespace gspec {
 
-__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return v;
-}
-
 // Same commit rule as the shared-memory path: per-pol n0, n1, s0, s1 to
 // pol_stats; n0, n1 summed over pols to the output record; saturation to sat[k].
+// A pass-A thread gathers at most four groups of at most 32 samples per pol
+// (|sample| <= 2048, so |sum| <= 2^18), and a CTA has at most 512 threads:
+// its counts and sums fit in 32 bits and each warp reduces them with one
+// redux.sync per value.
 template <int NPOL>
 __device__ void commit_stats(const ChainParams& p, const GateStats (&st)[NPOL], uint32_t k, int vals_c,
                        unsigned long long* red) {
   constexpr int NV = 4 * NPOL + 4;
-  unsigned long long v[NV];
-  unsigned long long n0 = 0, n1 = 0, s0 = 0, s1 = 0;
+  int v[NV];
+  uint32_t n0 = 0, n1 = 0, s0 = 0, s1 = 0;
 #pragma unroll
   for (int q = 0; q < NPOL; ++q) {
-    v[4 * q + 0] = st[q].n0;
-    v[4 * q + 1] = st[q].n1;
-    v[4 * q + 2] = static_cast<unsigned long long>(st[q].s0);
-    v[4 * q + 3] = static_cast<unsigned long long>(st[q].s1);
+    v[4 * q + 0] = static_cast<int>(st[q].n0);
+    v[4 * q + 1] = static_cast<int>(st[q].n1);
+    v[4 * q + 2] = static_cast<int>(st[q].s0);
+    v[4 * q + 3] = static_cast<int>(st[q].s1);
     n0 += st[q].n0;
     n1 += st[q].n1;
     s0 += st[q].sat0;
     s1 += st[q].sat1;
   }
-  v[4 * NPOL + 0] = n0;
-  v[4 * NPOL + 1] = n1;
-  v[4 * NPOL + 2] = s0;
-  v[4 * NPOL + 3] = s1;
+  v[4 * NPOL + 0] = static_cast<int>(n0);
+  v[4 * NPOL + 1] = static_cast<int>(n1);
+  v[4 * NPOL + 2] = static_cast<int>(s0);
+  v[4 * NPOL + 3] = static_cast<int>(s1);
+  int* red32 = reinterpret_cast<int*>(red);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
   for (int i = 0; i < NV; ++i) {
-    unsigned long long s = warp_sum_u64(v[i]);
-    if (lane == 0) red[warp * NV + i] = s;
+    const int s = __reduce_add_sync(0xffffffffu, v[i]);
+    if (lane == 0) red32[warp * NV + i] = s;
   }
   __syncthreads();
   if (threadIdx.x < NV) {
-    unsigned long long tot = 0;
-    for (int w = 0; w < nw; ++w) tot += red[w * NV + threadIdx.x];
+    long long tot = 0;
+    for (int w = 0; w < nw; ++w) tot += red32[w * NV + threadIdx.x];
     const int i = threadIdx.x;
     if (tot) {
+      const unsigned long long u = static_cast<unsigned long long>(tot);
       if (i < 4 * NPOL) {
-        atomicAdd(p.pol_stats + i, tot);
+        atomicAdd(p.pol_stats + i, u);
       } else if (i - 4 * NPOL < 2) {
         unsigned long long* cnt =
             reinterpret_cast<unsigned long long*>(p.out + k * p.out_rec + static_cast<uint64_t>(vals_c) * 4);
-        atomicAdd(cnt + (i - 4 * NPOL), tot);
+        atomicAdd(cnt + (i - 4 * NPOL), u);
       } else {
-        atomicAdd(p.sat + 2 * k + (i - 4 * NPOL - 2), tot);
+        atomicAdd(p.sat + 2 * k + (i - 4 * NPOL - 2), u);
       }
     }
   }

@@ -257,6 +257,8 @@ __global__ void __launch_bounds__(PassALayout::THREADS, 2) tc_a_kernel(FourStepP
   const int keep0 = static_cast<int>(c0 - gbase);
   const bool count_stats = G <= BC || c0 == gbase;
   const uint32_t sg_a = count_stats ? (DUAL ? (1u << ga) : 3u) : 0u;
+  static_assert((N1 + THREADS - 1) / THREADS * G <= 128 && THREADS <= 512,
+                "per-thread gate statistics fit the 32-bit commit");
   GateStats st[NPOL];
   for (int n1 = tid; n1 < N1; n1 += THREADS) {
     const uint32_t off = N2 * n1 + gbase;
