@@ -323,13 +323,21 @@ struct GateParams {
   uint32_t nbits;
   int32_t heap_shift;        // intended convention: log2(samples per heap) when that is an integer power of 2, else -1
   const uint8_t* masks;      // per item index: bit0 = gate 0 (m0), bit1 = gate 1 (m1); built by the mask pass
+  uint64_t heap_magic;       // ceil(2^64 / heap_size), 0 for heap_size 1 (see heap_of)
 };
+
+// n / heap_size for 32-bit n without a division: with M = ceil(2^64 / d) =
+// 2^64/d + e (0 <= e < 1), n*M/2^64 = n/d + n*e/2^64 and n*e/2^64 < 2^-32 < 1/d,
+// which never carries floor(n/d) past the next integer (d < 2^32).
+__device__ __forceinline__ uint32_t heap_of(const GateParams& g, uint32_t n) {
+  return g.heap_magic ? static_cast<uint32_t>(__umul64hi(n, g.heap_magic)) : n;
+}
 
 __device__ __forceinline__ uint32_t item_index(const GateParams& g, uint32_t s) {
   if (g.convention == 1) {
     const uint32_t j = s / g.chunk;
     const uint32_t t = s - j * g.chunk;
-    return j * g.step + (t / g.heap_size) * g.nsc + g.sel;
+    return j * g.step + heap_of(g, t) * g.nsc + g.sel;
   }
   if (g.heap_shift >= 0) return (s >> g.heap_shift) * g.nsc + g.sel;
   const uint64_t bit = static_cast<uint64_t>(s) * g.nbits;
@@ -337,11 +345,11 @@ __device__ __forceinline__ uint32_t item_index(const GateParams& g, uint32_t s) 
 }
 
 // Byte address of pol-stream byte b (dual-pol heaps alternate P0 P1).
-// (pol byte offsets are below 2^32, checked by the host, so 32-bit division)
+// (pol byte offsets are below 2^32, checked by the host, so heap_of applies)
 __device__ __forceinline__ const uint8_t* pol_byte(const GateParams& g, int pol, uint64_t b) {
   if (!g.dual) return g.block + b;
   const uint32_t b32 = static_cast<uint32_t>(b);
-  const uint32_t h = b32 / g.heap_size;
+  const uint32_t h = heap_of(g, b32);
   return g.block + (2ull * h + pol) * g.heap_size + (b32 - h * g.heap_size);
 }
 
@@ -496,6 +504,75 @@ __device__ __forceinline__ void gate_group1(const GateParams& g, int pol, uint32
       st.n0 += cnt;
       st.s0 += sumv;
       st.sat0 += satc;
+    }
+  }
+}
+
+// One gate of one group of both pols: re[] = pol 0, im[] = pol 1.  The pols
+// share the sample index, hence the (merged dual-pol) item and its masks, and
+// the heap pair: pol 1's bytes lie one heap after pol 0's.  Statistics of
+// pol 0 go to st0 and of pol 1 to st1 when `stats` is set.
+template <int NBITS>
+__device__ __forceinline__ void gate_group_dual(const GateParams& g, uint32_t s, float b0, float b1, int gate,
+                                                float (&re)[Group<NBITS>::samples],
+                                                float (&im)[Group<NBITS>::samples], GateStats& st0, GateStats& st1,
+                                                bool stats) {
+  constexpr int GS = Group<NBITS>::samples;
+  const uint32_t byte0 = static_cast<uint32_t>(static_cast<uint64_t>(s) * NBITS / 8);
+  const uint32_t h = heap_of(g, byte0);
+  const uint8_t* p0 = g.block + 2ull * h * g.heap_size + (byte0 - h * g.heap_size);
+  int v0[GS], v1[GS];
+  unpack_group<NBITS>(p0, v0);
+  unpack_group<NBITS>(p0 + g.heap_size, v1);
+  const uint32_t ia = item_index(g, s);
+  const uint32_t ib = item_index(g, s + GS - 1);
+  const uint32_t sh = gate ? 1u : 0u;
+  const bool ma = (__ldg(g.masks + ia) >> sh) & 1u;
+  constexpr int lo = -(1 << (NBITS - 1)), hi = (1 << (NBITS - 1)) - 1;
+  int sum0 = 0, sum1 = 0, sat0 = 0, sat1 = 0, cnt = 0;
+  if (ib == ia) {
+#pragma unroll
+    for (int i = 0; i < GS; ++i) {
+      re[i] = gate_value(static_cast<float>(v0[i]), b0, ma);
+      im[i] = gate_value(static_cast<float>(v1[i]), b1, ma);
+      sum0 += v0[i];
+      sum1 += v1[i];
+      sat0 += (v0[i] == lo) | (v0[i] == hi);
+      sat1 += (v1[i] == lo) | (v1[i] == hi);
+    }
+    cnt = ma ? GS : 0;
+    if (!ma) sum0 = sum1 = sat0 = sat1 = 0;
+  } else {
+    const bool mb = (__ldg(g.masks + ib) >> sh) & 1u;
+    uint32_t boundary = s;
+    while (boundary < s + GS && item_index(g, boundary) == ia) ++boundary;
+#pragma unroll
+    for (int i = 0; i < GS; ++i) {
+      const bool m = (s + i) >= boundary ? mb : ma;
+      re[i] = gate_value(static_cast<float>(v0[i]), b0, m);
+      im[i] = gate_value(static_cast<float>(v1[i]), b1, m);
+      cnt += m;
+      sum0 += m ? v0[i] : 0;
+      sum1 += m ? v1[i] : 0;
+      sat0 += m && ((v0[i] == lo) | (v0[i] == hi));
+      sat1 += m && ((v1[i] == lo) | (v1[i] == hi));
+    }
+  }
+  if (stats) {
+    if (gate) {
+      st0.n1 += cnt;
+      st0.s1 += sum0;
+      st0.sat1 += sat0;
+      st1.n1 += cnt;
+      st1.s1 += sum1;
+      st1.sat1 += sat1;
+    } else {
+      st0.n0 += cnt;
+      st0.s0 += sum0;
+      st0.sat0 += sat0;
+      st1.n0 += cnt;
+      st1.s0 += sum1;
+      st1.sat0 += sat1;
     }
   }
 }

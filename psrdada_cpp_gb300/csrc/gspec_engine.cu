@@ -166,6 +166,7 @@ GateParams gate_params(const gspec_handle* h, const uint8_t* block) {
   g.block = block;
   g.sc_offset = h->sc_off;
   g.heap_size = static_cast<uint32_t>(h->cfg.heap_size);
+  g.heap_magic = g.heap_size > 1 ? UINT64_MAX / g.heap_size + 1 : 0;   // ceil(2^64 / heap_size)
   g.nsc = static_cast<uint32_t>(h->cfg.n_side_channels);
   g.sel = static_cast<uint32_t>(h->cfg.selected_side_channel);
   g.bitpos = static_cast<uint32_t>(h->cfg.selected_bit);

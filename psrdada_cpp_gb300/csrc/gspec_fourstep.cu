@@ -91,8 +91,7 @@ __global__ void __launch_bounds__(PassACfg<N1>::THREADS) fourstep_a_kernel(FourS
     const uint32_t off = N2 * n1 + gs;
     float re[G], im[G];
     if constexpr (DUAL) {
-      gate_group1<NBITS>(p.c.g, 0, frA * N + off, bl[ga], ga, re, st[0], count_stats);
-      gate_group1<NBITS>(p.c.g, 1, frA * N + off, bl[2 + ga], ga, im, st[NPOL - 1], count_stats);
+      gate_group_dual<NBITS>(p.c.g, frA * N + off, bl[ga], bl[2 + ga], ga, re, im, st[0], st[NPOL - 1], count_stats);
     } else if (fb == fa) {
       gate_group<NBITS>(p.c.g, 0, frA * N + off, bl[0], bl[1], re, im, st[0], sg_a);
     } else {

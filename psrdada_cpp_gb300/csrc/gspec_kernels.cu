@@ -186,8 +186,7 @@ __global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS, GSPEC_SMALL_MINB)
         const uint32_t sa = (f0 + fa) * N + gi * G;
         float re[G], im[G];
         if constexpr (DUAL) {
-          gate_group1<NBITS>(p.g, 0, sa, bl[ga], ga, re, st[0], true);
-          gate_group1<NBITS>(p.g, 1, sa, bl[2 + ga], ga, im, st[NPOL - 1], true);
+          gate_group_dual<NBITS>(p.g, sa, bl[ga], bl[2 + ga], ga, re, im, st[0], st[NPOL - 1], true);
         } else if (fb == fa) {
           gate_group<NBITS>(p.g, 0, sa, bl[0], bl[1], re, im, st[0], 3u);
         } else {
