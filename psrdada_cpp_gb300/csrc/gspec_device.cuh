@@ -297,6 +297,30 @@ __device__ __forceinline__ void unpack_group(const uint8_t* __restrict__ p, int 
   }
 }
 
+// Unpack S samples that start on a 4-byte boundary (S * NBITS a multiple of
+// 32 bits): the part of a group that a tile narrower than the group keeps.
+template <int NBITS, int S>
+__device__ __forceinline__ void unpack_span(const uint8_t* __restrict__ p, int (&out)[S]) {
+  if constexpr (S == Group<NBITS>::samples) {
+    unpack_group<NBITS>(p, out);
+  } else {
+    static_assert((S * NBITS) % 32 == 0, "a span is whole 32-bit words");
+    constexpr int NW = S * NBITS / 32;
+    uint32_t W[NW + 1];
+    const uint32_t* q = reinterpret_cast<const uint32_t*>(p);
+#pragma unroll
+    for (int w = 0; w < NW; ++w) W[w] = bswap32(__ldg(q + w));
+    W[NW] = 0;
+#pragma unroll
+    for (int i = 0; i < S; ++i) {
+      const int bit = NBITS * i;
+      const int w = bit >> 5, sh = bit & 31;
+      const uint32_t win = __funnelshift_l(W[w + 1], W[w], sh);
+      out[i] = static_cast<int32_t>(win) >> (32 - NBITS);
+    }
+  }
+}
+
 // ---------------------------------------------------------------- gating
 // Side-channel gate of one sample (edd/src/GatedSpectrometer.cu:49-52):
 //   G1 = (v - b1) * bit * !lost + b1 ;  G0 = (v - b0) * !bit * !lost + b0
@@ -394,14 +418,13 @@ __device__ __forceinline__ void mask_of(const GateParams& g, uint32_t idx, bool&
 // Writes gated G0/G1 floats into g0[], g1[]; adds the statistics of gate 0
 // when (stat_gates & 1) and of gate 1 when (stat_gates & 2), so that a
 // sample visited by two jobs is counted once.
-template <int NBITS>
+template <int NBITS, int GS = Group<NBITS>::samples>
 __device__ __forceinline__ void gate_group(const GateParams& g, int pol, uint32_t s, float b0, float b1,
-                                           float (&g0)[Group<NBITS>::samples], float (&g1)[Group<NBITS>::samples],
+                                           float (&g0)[GS], float (&g1)[GS],
                                            GateStats& st, uint32_t stat_gates = 3u) {
-  constexpr int GS = Group<NBITS>::samples;
   int v[GS];
   const uint64_t byte0 = static_cast<uint64_t>(s) * NBITS / 8;
-  unpack_group<NBITS>(pol_byte(g, pol, byte0), v);
+  unpack_span<NBITS, GS>(pol_byte(g, pol, byte0), v);
   const uint32_t ia = item_index(g, s);
   const uint32_t ib = item_index(g, s + GS - 1);
   bool a0, a1;
@@ -460,13 +483,12 @@ __device__ __forceinline__ void gate_group(const GateParams& g, int pol, uint32_
 
 // One gate of one group: out[] = gate `gate` of the samples; statistics of
 // that gate only when `stats` is set.
-template <int NBITS>
+template <int NBITS, int GS = Group<NBITS>::samples>
 __device__ __forceinline__ void gate_group1(const GateParams& g, int pol, uint32_t s, float b, int gate,
-                                            float (&out)[Group<NBITS>::samples], GateStats& st, bool stats) {
-  constexpr int GS = Group<NBITS>::samples;
+                                            float (&out)[GS], GateStats& st, bool stats) {
   int v[GS];
   const uint64_t byte0 = static_cast<uint64_t>(s) * NBITS / 8;
-  unpack_group<NBITS>(pol_byte(g, pol, byte0), v);
+  unpack_span<NBITS, GS>(pol_byte(g, pol, byte0), v);
   const uint32_t ia = item_index(g, s);
   const uint32_t ib = item_index(g, s + GS - 1);
   const uint32_t sh = gate ? 1u : 0u;
@@ -512,18 +534,16 @@ __device__ __forceinline__ void gate_group1(const GateParams& g, int pol, uint32
 // share the sample index, hence the (merged dual-pol) item and its masks, and
 // the heap pair: pol 1's bytes lie one heap after pol 0's.  Statistics of
 // pol 0 go to st0 and of pol 1 to st1 when `stats` is set.
-template <int NBITS>
+template <int NBITS, int GS = Group<NBITS>::samples>
 __device__ __forceinline__ void gate_group_dual(const GateParams& g, uint32_t s, float b0, float b1, int gate,
-                                                float (&re)[Group<NBITS>::samples],
-                                                float (&im)[Group<NBITS>::samples], GateStats& st0, GateStats& st1,
+                                                float (&re)[GS], float (&im)[GS], GateStats& st0, GateStats& st1,
                                                 bool stats) {
-  constexpr int GS = Group<NBITS>::samples;
   const uint32_t byte0 = static_cast<uint32_t>(static_cast<uint64_t>(s) * NBITS / 8);
   const uint32_t h = heap_of(g, byte0);
   const uint8_t* p0 = g.block + 2ull * h * g.heap_size + (byte0 - h * g.heap_size);
   int v0[GS], v1[GS];
-  unpack_group<NBITS>(p0, v0);
-  unpack_group<NBITS>(p0 + g.heap_size, v1);
+  unpack_span<NBITS, GS>(p0, v0);
+  unpack_span<NBITS, GS>(p0 + g.heap_size, v1);
   const uint32_t ia = item_index(g, s);
   const uint32_t ib = item_index(g, s + GS - 1);
   const uint32_t sh = gate ? 1u : 0u;

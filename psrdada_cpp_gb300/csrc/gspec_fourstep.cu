@@ -74,39 +74,43 @@ __global__ void __launch_bounds__(PassACfg<N1>::THREADS) fourstep_a_kernel(FourS
   for (int i = 0; i < 2 * NPOL; ++i) bl[i] = p.c.baselines[i];
   load_twiddles<N1>(tws, p.tw1);
 
-  // groups covering this tile's columns of one row
-  constexpr int GPR = G <= BC ? BC / G : 1;
-  const uint32_t gbase = G <= BC ? c0 : (c0 / G) * G;
-  const int keep0 = static_cast<int>(c0 - gbase);        // first kept element of a group
-  const bool count_stats = (c0 == gbase || G <= BC);
+  // spans of SP samples covering this tile's columns of one row: whole
+  // groups, or only the tile's part of a group when that part is whole
+  // 32-bit words (12-bit samples, 8-column tiles)
+  constexpr int SP = (G > BC && (BC * NBITS) % 32 == 0) ? BC : G;
+  constexpr int GPR = SP <= BC ? BC / SP : 1;
+  const uint32_t gbase = SP <= BC ? c0 : (c0 / SP) * SP;
+  const int keep0 = static_cast<int>(c0 - gbase);        // first kept element of a span
+  const bool count_stats = (c0 == gbase || SP <= BC);
   const uint32_t sg_a = count_stats ? (DUAL ? (1u << ga) : 3u) : 0u;
 
-  static_assert((N1 * GPR + Cfg::THREADS - 1) / Cfg::THREADS * G <= 128 && Cfg::THREADS <= 512,
+  static_assert((N1 * GPR + Cfg::THREADS - 1) / Cfg::THREADS * SP <= 128 && Cfg::THREADS <= 512,
                 "per-thread gate statistics fit the 32-bit commit");
   GateStats st[NPOL];
   for (int w = tid; w < N1 * GPR; w += Cfg::THREADS) {
     const int n1 = w % N1;
     const int gi = w / N1;
-    const uint32_t gs = gbase + gi * G;
+    const uint32_t gs = gbase + gi * SP;
     const uint32_t off = N2 * n1 + gs;
-    float re[G], im[G];
+    float re[SP], im[SP];
     if constexpr (DUAL) {
-      gate_group_dual<NBITS>(p.c.g, frA * N + off, bl[ga], bl[2 + ga], ga, re, im, st[0], st[NPOL - 1], count_stats);
+      gate_group_dual<NBITS, SP>(p.c.g, frA * N + off, bl[ga], bl[2 + ga], ga, re, im, st[0], st[NPOL - 1],
+                                 count_stats);
     } else if (fb == fa) {
-      gate_group<NBITS>(p.c.g, 0, frA * N + off, bl[0], bl[1], re, im, st[0], sg_a);
+      gate_group<NBITS, SP>(p.c.g, 0, frA * N + off, bl[0], bl[1], re, im, st[0], sg_a);
     } else {
-      gate_group1<NBITS>(p.c.g, 0, frA * N + off, bl[ga], ga, re, st[0], count_stats);
+      gate_group1<NBITS, SP>(p.c.g, 0, frA * N + off, bl[ga], ga, re, st[0], count_stats);
       if (fb != kNoFrame) {
-        gate_group1<NBITS>(p.c.g, 0, frB * N + off, bl[gb], gb, im, st[0], count_stats);
+        gate_group1<NBITS, SP>(p.c.g, 0, frB * N + off, bl[gb], gb, im, st[0], count_stats);
       } else {
 #pragma unroll
-        for (int e = 0; e < G; ++e) im[e] = 0.f;
+        for (int e = 0; e < SP; ++e) im[e] = 0.f;
       }
     }
 #pragma unroll
-    for (int e = 0; e < G; ++e) {
+    for (int e = 0; e < SP; ++e) {
       const int col = static_cast<int>(gs - c0) + e;
-      if (G <= BC || (e >= keep0 && e < keep0 + BC)) S[col * Cfg::STRIDE + spad(n1)] = make_float2(re[e], im[e]);
+      if (SP <= BC || (e >= keep0 && e < keep0 + BC)) S[col * Cfg::STRIDE + spad(n1)] = make_float2(re[e], im[e]);
     }
   }
   __syncthreads();

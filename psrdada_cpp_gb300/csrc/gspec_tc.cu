@@ -253,31 +253,36 @@ __global__ void __launch_bounds__(PassALayout::THREADS, 2) tc_a_kernel(FourStepP
   // unpack + gate the 8 columns of every row (one group per row) into the
   // stage-1 operands of both tiles
   constexpr float sc1 = Scales<BF16>::a1, sc2 = Scales<BF16>::a2;
-  const uint32_t gbase = G <= BC ? c0 : (c0 / G) * G;
+  // one span per row: the whole group, or the tile's part of it when that
+  // part is whole 32-bit words (12-bit samples)
+  constexpr int SP = (G > BC && (BC * NBITS) % 32 == 0) ? BC : G;
+  static_assert(SP >= BC, "one span covers the tile's columns");
+  const uint32_t gbase = SP <= BC ? c0 : (c0 / SP) * SP;
   const int keep0 = static_cast<int>(c0 - gbase);
-  const bool count_stats = G <= BC || c0 == gbase;
+  const bool count_stats = SP <= BC || c0 == gbase;
   const uint32_t sg_a = count_stats ? (DUAL ? (1u << ga) : 3u) : 0u;
-  static_assert((N1 + THREADS - 1) / THREADS * G <= 128 && THREADS <= 512,
+  static_assert((N1 + THREADS - 1) / THREADS * SP <= 128 && THREADS <= 512,
                 "per-thread gate statistics fit the 32-bit commit");
   GateStats st[NPOL];
   for (int n1 = tid; n1 < N1; n1 += THREADS) {
     const uint32_t off = N2 * n1 + gbase;
-    float re[G], im[G];
+    float re[SP], im[SP];
     if constexpr (DUAL) {
-      gate_group_dual<NBITS>(p.c.g, frA * N + off, bl[ga], bl[2 + ga], ga, re, im, st[0], st[NPOL - 1], count_stats);
+      gate_group_dual<NBITS, SP>(p.c.g, frA * N + off, bl[ga], bl[2 + ga], ga, re, im, st[0], st[NPOL - 1],
+                                 count_stats);
     } else if (fb == fa) {
-      gate_group<NBITS>(p.c.g, 0, frA * N + off, bl[0], bl[1], re, im, st[0], sg_a);
+      gate_group<NBITS, SP>(p.c.g, 0, frA * N + off, bl[0], bl[1], re, im, st[0], sg_a);
     } else {
-      gate_group1<NBITS>(p.c.g, 0, frA * N + off, bl[ga], ga, re, st[0], count_stats);
+      gate_group1<NBITS, SP>(p.c.g, 0, frA * N + off, bl[ga], ga, re, st[0], count_stats);
       if (fb != kNoFrame) {
-        gate_group1<NBITS>(p.c.g, 0, frB * N + off, bl[gb], gb, im, st[0], count_stats);
+        gate_group1<NBITS, SP>(p.c.g, 0, frB * N + off, bl[gb], gb, im, st[0], count_stats);
       } else {
 #pragma unroll
-        for (int e = 0; e < G; ++e) im[e] = 0.f;
+        for (int e = 0; e < SP; ++e) im[e] = 0.f;
       }
     }
 #pragma unroll
-    for (int e = 0; e < G; ++e) {
+    for (int e = 0; e < SP; ++e) {
       const int col = e - keep0;
       if (col >= 0 && col < BC) put_stage1<BF16>(col < 4 ? s0 : s1, col & 3, n1, make_float2(re[e], im[e]), sc1);
     }
