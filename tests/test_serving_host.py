@@ -6,6 +6,7 @@ entry points fail loudly without a device."""
 import ctypes
 import subprocess
 
+import numpy as np
 import pytest
 
 import psrdada_cpp_gb300 as G
@@ -126,3 +127,31 @@ def test_burst_plan_interleaves_streams():
     from psrdada_cpp_gb300 import loadgen
     plan = loadgen.burst_plan([synth.config1(), synth.config2()], [3, 2])
     assert [i for _, i in plan] == [0, 1, 0, 1, 0] and all(t == 0.0 for t, _ in plan)
+
+
+def test_latency_summary_splits_stages():
+    """Per-shape percentiles of the block latency and of each recorded stage,
+    and p99 over the block span, from synthetic records."""
+    from psrdada_cpp_gb300 import loadgen
+    specs = [synth.config1(), synth.config3()]
+    rows = []
+    for k in range(100):
+        for i in (0, 1):
+            t_sub = 0.01 * k
+            lat = (1.0 + (k % 10)) * 1e-3 * (1 + 9 * i)        # long blocks take 10x as long
+            # stream, block, t_submit, t_start, t_done, h2d, wait, chain, d2h, issue, observe (ms)
+            rows.append((i, k, t_sub, t_sub + 1e-4, t_sub + lat, 0.1, 0.0, 0.2 * (1 + i), 0.05, 0.02, 0.01))
+    res = {"records": np.array(rows)}
+    rate = 1e9
+    out = loadgen.latency_summary(res, specs, rate)
+    assert out["blocks"] == 200
+    short, long_ = out["by_shape"][specs[0].name], out["by_shape"][specs[1].name]
+    assert short["blocks"] == long_["blocks"] == 100
+    assert abs(short["p50_ms"] - np.percentile([(1.0 + k % 10) for k in range(100)], 50)) < 1e-9
+    assert abs(long_["p99_ms"] / short["p99_ms"] - 10.0) < 1e-9
+    assert short["chain_p50_ms"] == pytest.approx(0.2) and long_["chain_p50_ms"] == pytest.approx(0.4)
+    assert short["issue_p99_ms"] == pytest.approx(0.02) and short["observe_p50_ms"] == pytest.approx(0.01)
+    assert short["queue_p50_ms"] == pytest.approx(0.1)
+    span_ms = loadgen.block_samples(specs[0]) / rate * 1e3
+    assert short["block_span_ms"] == pytest.approx(span_ms)
+    assert short["p99_over_span"] == pytest.approx(short["p99_ms"] / span_ms)
