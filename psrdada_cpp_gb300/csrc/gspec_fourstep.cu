@@ -43,7 +43,7 @@ struct PassACfg {
 
 // grid.x = nk * maxjobs * (N2 / BC): (output spectrum, job, column tile)
 template <int N1, int NBITS, bool DUAL>
-__global__ void __launch_bounds__(PassACfg<N1>::THREADS) fourstep_a_kernel(FourStepParams p) {
+__device__ __forceinline__ void fourstep_a_body(const FourStepParams& p) {
   using Cfg = PassACfg<N1>;
   constexpr int BC = Cfg::BC;
   constexpr int G = Group<NBITS>::samples;
@@ -141,6 +141,20 @@ __global__ void __launch_bounds__(PassACfg<N1>::THREADS) fourstep_a_kernel(FourS
     }
   }
   commit_stats<NPOL>(p.c, st, k, (DUAL ? 8 : 2) * static_cast<int>(N / 2 + 1), red);
+}
+
+template <int N1, int NBITS, bool DUAL>
+__global__ void __launch_bounds__(PassACfg<N1>::THREADS) fourstep_a_kernel(FourStepParams p) {
+  fourstep_a_body<N1, NBITS, DUAL>(p);
+}
+
+// The same pass held to 64 registers so that two 512-thread CTAs share an SM.
+#ifndef GSPEC_PASSA_2CTA
+#define GSPEC_PASSA_2CTA 1
+#endif
+template <int N1, int NBITS, bool DUAL>
+__global__ void __launch_bounds__(PassACfg<N1>::THREADS, 2) fourstep_a_2cta_kernel(FourStepParams p) {
+  fourstep_a_body<N1, NBITS, DUAL>(p);
 }
 
 #ifndef GSPEC_PASSB_THREADS
@@ -406,10 +420,21 @@ static cudaError_t launch_a_n1(int nbits, const FourStepParams& p, cudaStream_t 
     kern<<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(p);
     return cudaGetLastError();
   };
-  switch (nbits) {
-    case 8: return run(fourstep_a_kernel<N1, 8, DUAL>);
-    case 10: return run(fourstep_a_kernel<N1, 10, DUAL>);
-    case 12: return run(fourstep_a_kernel<N1, 12, DUAL>);
+  // 1024-point columns (512 threads) at 78 registers leave one CTA per SM;
+  // held to 64 they fit two (8- and 12-bit; 10-bit, and 512-point columns,
+  // would spill)
+  if constexpr (GSPEC_PASSA_2CTA && N1 == 1024) {
+    switch (nbits) {
+      case 8: return run(fourstep_a_2cta_kernel<N1, 8, DUAL>);
+      case 10: return run(fourstep_a_kernel<N1, 10, DUAL>);
+      case 12: return run(fourstep_a_2cta_kernel<N1, 12, DUAL>);
+    }
+  } else {
+    switch (nbits) {
+      case 8: return run(fourstep_a_kernel<N1, 8, DUAL>);
+      case 10: return run(fourstep_a_kernel<N1, 10, DUAL>);
+      case 12: return run(fourstep_a_kernel<N1, 12, DUAL>);
+    }
   }
   return cudaErrorInvalidValue;
 }
