@@ -142,8 +142,11 @@ class Server:
         return self._lib.gspec_stream_state(self._s, stream)
 
     def submit(self, stream: int, block, tag: int) -> None:
-        """``block``: a numpy uint8 array (pinned via torch for overlap) or a
-        (pointer, size) pair; ``tag`` identifies the block in its result."""
+        """``block``: a numpy uint8 array, a torch tensor or a (pointer, size)
+        pair; ``tag`` identifies the block in its result.  Page-locked blocks
+        (e.g. ``torch.empty(..., pin_memory=True)``) overlap their copy with
+        other streams' work, and up to 64 MiB are read by SM loads, never
+        queueing behind other streams' copies."""
         if isinstance(block, tuple):
             ptr, size = block
         elif isinstance(block, np.ndarray):
