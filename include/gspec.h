@@ -147,7 +147,8 @@ int gspec_process_device(gspec_handle* h, const void* d_block, size_t used_bytes
  * caller-owned device output buffer (gspec_info.output_bytes without the
  * saturation record, host layout), on the caller's CUDA stream; updates the
  * baselines.  No handler pipeline, no host copies.  The caller zeroes d_out
- * at the start of an output block. */
+ * at the start of an output block.  d_block and d_out are 16-byte aligned
+ * (GSPEC_ERR_ARG otherwise). */
 int gspec_run_block_device(gspec_handle* h, const void* d_block, void* d_out, void* cuda_stream);
 
 int gspec_get_info(const gspec_handle* h, gspec_info* info);
@@ -181,7 +182,8 @@ int gspec_get_saturation(gspec_handle* h, uint64_t* out);
  * device memory through the chain, accumulated into the caller's d_out
  * (output layout without the saturation record), with the caller's
  * d_baselines (4 floats [pol][G0, G1], read and updated for the next block)
- * on the caller's stream.  No handle, no cudaMalloc/cudaFree: the working
+ * on the caller's stream (d_block and d_out 16-byte aligned, d_baselines
+ * 4-byte; GSPEC_ERR_ARG otherwise).  No handle, no cudaMalloc/cudaFree: the working
  * memory is a library-owned device array of GSPEC_NOALLOC_SCRATCH_BYTES held
  * by every GPU that loads the library.  Only fft_length <= 4096; larger
  * working sets are rejected (GSPEC_ERR_UNSUPPORTED) with the reason in err.

@@ -690,6 +690,9 @@ int gspec_process_device(gspec_handle* h, const void* d_block, size_t used_bytes
 
 int gspec_run_block_device(gspec_handle* h, const void* d_block, void* d_out, void* cuda_stream) {
   if (!h || !d_block || !d_out) return GSPEC_ERR_ARG;
+  // the kernels read the block in 8-byte words and add 8-byte counters to d_out
+  if ((reinterpret_cast<uintptr_t>(d_block) | reinterpret_cast<uintptr_t>(d_out)) % 16)
+    return set_err(h, GSPEC_ERR_ARG, "d_block and d_out must be 16-byte aligned");
   if (device_error(h) != GSPEC_OK) return GSPEC_ERR_CUDA;
   cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
   if (!cuda_ok(h, launch_chain(h, static_cast<const uint8_t*>(d_block), static_cast<uint8_t*>(d_out), h->d_sat_dev, s),

@@ -603,7 +603,8 @@ __global__ void copy_quads_kernel(const uint4* src, uint4* dst, uint64_t n) {
 }
 
 cudaError_t launch_copy_words(void* dst, const void* src, uint64_t bytes, int sm_count, cudaStream_t s) {
-  if (bytes % 8) return cudaErrorInvalidValue;
+  if (bytes % 8 || (reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) % 8)
+    return cudaErrorInvalidValue;   // 8-byte words only
   const bool quads = bytes % 16 == 0 && reinterpret_cast<uintptr_t>(dst) % 16 == 0 &&
                      reinterpret_cast<uintptr_t>(src) % 16 == 0;
   const uint64_t n = bytes / (quads ? 16 : 8);

@@ -59,6 +59,10 @@ size_t align256(size_t n) { return (n + 255) & ~static_cast<size_t>(255); }
 extern "C" int gspec_process_block_noalloc(const gspec_config* cfg, const void* d_block, float* d_baselines,
                                            void* d_out, void* cuda_stream, char* err, size_t err_len) {
   if (!cfg || !d_block || !d_baselines || !d_out) return fail(err, err_len, GSPEC_ERR_ARG, "null argument");
+  // the kernels read the block in 8-byte words and add 8-byte counters to d_out
+  if ((reinterpret_cast<uintptr_t>(d_block) | reinterpret_cast<uintptr_t>(d_out)) % 16 ||
+      reinterpret_cast<uintptr_t>(d_baselines) % 4)
+    return fail(err, err_len, GSPEC_ERR_ARG, "d_block and d_out must be 16-byte aligned, d_baselines 4-byte");
   gspec_handle h;  // stack description only: no buffer of its own
   h.cfg = *cfg;
   if (!gspec_engine::configure_handle(&h)) return fail(err, err_len, GSPEC_ERR_ARG, h.err.c_str());

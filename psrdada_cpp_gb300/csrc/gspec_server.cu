@@ -243,7 +243,8 @@ bool issue(gspec_server* s, Stream& st, const Queued& q, int obuf) {
   const int es = st.ev_next;
   Flight f{q.index, q.tag, q.t_submit, now_s(s), obuf, st.ev[es], q.size > kShortBlockMax ? q.size : 0, es};
   st.ev_next = (st.ev_next + 1) % kEventsPerStream;
-  const void* src_dev = q.size <= kShortBlockMax && q.size % 8 == 0 ? mapped_host(q.data) : nullptr;
+  const bool words = q.size % 8 == 0 && reinterpret_cast<uintptr_t>(q.data) % 8 == 0;
+  const void* src_dev = q.size <= kShortBlockMax && words ? mapped_host(q.data) : nullptr;
   if (src_dev) {
     // the compute stream's earlier chains are the input slot's only readers
     if (!ok(st, cudaEventRecord(st.ev_stage[0][es], h->proc), "record") ||

@@ -63,6 +63,24 @@ def test_configuration_errors_without_gpu():
     assert "cudaSetDevice" in msg or "CUDA" in msg or msg == ""
 
 
+def test_misaligned_device_pointers_are_rejected_before_cuda():
+    """An unaligned block or output pointer is an argument error, found on the
+    host before any CUDA call (so no kernel ever reads it)."""
+    from psrdada_cpp_gb300.gated_spectrometer import GspecConfig, load_library
+    lib = load_library()
+    err = ctypes.create_string_buffer(256)
+    cfg = GspecConfig(buffer_size=16 * 4104, heap_size=4096, n_side_channels=1, fft_length=1024, naccumulate=4,
+                      nbits=8)
+    fn = lib.gspec_process_block_noalloc
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                   ctypes.c_char_p, ctypes.c_size_t]
+    aligned, odd = 1 << 20, (1 << 20) + 8
+    for blk, out in ((odd, aligned), (aligned, odd)):
+        rc = fn(ctypes.byref(cfg), blk, aligned, out, None, err, 256)
+        assert rc == -1 and b"aligned" in err.value, (rc, err.value)
+    assert lib.gspec_run_block_device(None, aligned, aligned, None) == -1   # null handle
+
+
 def test_python_mirror_fails_loudly_without_library(tmp_path):
     code = (
         "import psrdada_cpp_gb300.gated_spectrometer as g, pathlib;"
