@@ -49,7 +49,9 @@ def test_configuration_errors_without_gpu():
                     nbits=8)
         base.update(kw)
         h = lib.gspec_create(ctypes.byref(GspecConfig(**base)), err, 256)
-        assert not h
+        if h:                      # only a valid configuration on a machine with a GPU
+            lib.gspec_destroy(h)
+            return None
         return err.value.decode()
 
     assert "nbits" in create(nbits=16)
@@ -58,9 +60,9 @@ def test_configuration_errors_without_gpu():
     assert "multiple" in create(naccumulate=3)
     assert "selected_side_channel" in create(selected_side_channel=2)
     assert "tile" in create(convention=1, heap_size=8192, buffer_size=16 * 8200)
-    # a valid configuration only fails where CUDA starts (no GPU in this container)
+    # a valid configuration fails only where CUDA starts (on a machine without a GPU)
     msg = create()
-    assert "cudaSetDevice" in msg or "CUDA" in msg or msg == ""
+    assert msg is None or "cudaSetDevice" in msg or "CUDA" in msg or msg == ""
 
 
 def test_misaligned_device_pointers_are_rejected_before_cuda():
