@@ -7,7 +7,8 @@
 // takes them as a pair, splits the packed real sequences and accumulates the
 // power (edd/DetectorAccumulator.cuh:40-61) or Stokes
 // (edd/src/GatedSpectrometer.cu:140-169) spectra over the jobs of one output
-// spectrum before writing them once.
+// spectrum, then writes the pair's sums contiguously; the scatter kernel adds
+// them into the output record's bins (k1 + N1*k2) with coalesced accesses.
 //
 // The plan kernel builds each output spectrum's job list (build_jobs): only
 // gates holding data are transformed; gates without data add their constant
