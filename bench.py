@@ -1,10 +1,15 @@
 """Throughput benchmark of the GB300 gated spectrometer.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c2|c1|c3|c4|c5] [--impl gb300|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c3|c1|c2|c2m|c4|c5]
+                    [--form bf16|fp16|fp32] [--impl gb300|reference]
 
 One step = one DADA block of the workload through the whole chain (unpack,
 gate, R2C, Stokes/power accumulate).  Default workload: dual-pol 12-bit gated
-Stokes, fft 2^16, naccumulate 32, 2^26 samples per pol per block.
+Stokes, fft 2^20 (four-step 1024 x 1024), naccumulate 8, 2^28 samples per pol
+per block; the BF16 split-precision tensor-core form is ``value`` and the
+plain FP32 form is timed on the same blocks in the same run (``forms``,
+``tc_over_fp32``, and the two forms' spectral difference
+``tc_vs_fp32_spectra``).
 
 * ``value``   device throughput, input Gsamples/s (both pols), inputs resident
               in HBM: K blocks through gspec_run_block_device on the stream
@@ -57,11 +62,17 @@ L2_FALLBACK = 129 * 2**20                            # GB300 L2 size when the de
 
 # ------------------------------------------------------------------ helpers
 def workload(name: str):
+    import dataclasses
     from psrdada_cpp_gb300 import synth
     if name == "c1":
         return synth.config1(), "c1"
     if name == "c3":
         return synth.config3(), "c3"
+    if name == "c2m":
+        # the diode period (61 heaps of 4096 samples) is not a whole number of 2^16-sample frames:
+        # frames straddling a toggle hold data in both gates, the others in one
+        c2 = synth.config2()
+        return dataclasses.replace(c2, name=c2.name + "_diode61", diode_period_heaps=61), "c2"
     return synth.config2(), "c2"
 
 
@@ -142,63 +153,122 @@ def ncu_traffic(kernel: str, workload_name: str):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled while running."""
+    """SM clock, power and clock-event (throttle) reasons sampled while the
+    GPU works: read-only NVML queries through ctypes every 20 ms on a host
+    thread, or, where NVML cannot be loaded, one-shot nvidia-smi queries.
+    Start it before the warm-up and stop it after the last GPU phase so a
+    short timed region still has samples on both sides."""
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # NVML clock-event reason bits (nvml.h: nvmlClocksEventReason*)
+    BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40,
+            "hw_power_brake_slowdown": 0x80}
 
-    def __init__(self, index: int):
+    def __init__(self, index: int, pci_bus_id: str | None = None, period_s: float = 0.02):
         self.index = index
-        self.proc = None
-        self.lines = []
+        self.pci = pci_bus_id
+        self.period = period_s
+        self.samples = []            # (time, sm_mhz, max_mhz, power_w, set of reasons)
+        self.source = None
+        self._stop = threading.Event()
         self.thread = None
 
-    def start(self):
+    def _nvml(self):
+        import ctypes
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        h = ctypes.c_void_p()
+        ok = False
+        if self.pci:
+            ok = lib.nvmlDeviceGetHandleByPciBusId_v2(self.pci.encode(), ctypes.byref(h)) == 0
+        if not ok and lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.index), ctypes.byref(h)) != 0:
+            raise OSError("no NVML handle")
         try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
-                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-        except OSError:
-            self.proc = None
-            return
-        self.thread = threading.Thread(target=self._read, daemon=True)
-        self.thread.start()
+            reasons_fn = lib.nvmlDeviceGetCurrentClocksEventReasons
+        except AttributeError:
+            reasons_fn = lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        clk, mx, pw, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx))          # NVML_CLOCK_SM = 1
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append((time.time(), line.strip()))
+        def read():
+            lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk))
+            lib.nvmlDeviceGetPowerUsage(h, ctypes.byref(pw))
+            reasons_fn(h, ctypes.byref(rs))
+            names = {n for n, b in self.BITS.items() if rs.value & b}
+            return float(clk.value), float(mx.value), pw.value / 1000.0, names
+        read()
+        return read
+
+    def _smi(self):
+        def read():
+            out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                                  "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                 timeout=5).stdout
+            f = [x.strip() for x in out.strip().split(",")]
+            names = {n for n, v in zip(["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                                        "sw_power_cap"], f[5:9]) if v.lower() == "active"}
+            return float(f[1]), float(f[2]), float(f[3]) if f[3] not in ("", "[N/A]") else 0.0, names
+        read()
+        return read
+
+    def start(self):
+        read = None
+        for name, mk in (("nvml", self._nvml), ("nvidia-smi", self._smi)):
+            try:
+                read = mk()
+                self.source = name
+                break
+            except Exception:
+                continue
+        if read is None:
+            return
+
+        def loop():
+            while not self._stop.is_set():
+                try:
+                    t = time.time()
+                    self.samples.append((t,) + read())
+                except Exception:
+                    pass
+                self._stop.wait(self.period)
+        self.thread = threading.Thread(target=loop, daemon=True)
+        self.thread.start()
+        t0 = time.time()
+        while not self.samples and time.time() - t0 < 5:
+            time.sleep(0.01)
 
     def stop(self):
-        if self.proc:
-            self.proc.terminate()
-            try:
-                self.proc.wait(timeout=5)
-            except subprocess.TimeoutExpired:
-                self.proc.kill()
+        self._stop.set()
         if self.thread:
-            self.thread.join(timeout=2)
+            self.thread.join(timeout=5)
 
-    def summary(self, t0: float, t1: float):
-        sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ts, line in self.lines:
-            if not (t0 <= ts <= t1 + 0.06):
-                continue
-            f = [x.strip() for x in line.split(",")]
-            if len(f) < 9:
-                continue
-            try:
-                sm.append(float(f[1]))
-                mx.append(float(f[2]))
-            except ValueError:
-                continue
-            for n, v in zip(names, f[5:9]):
-                if v.lower() == "active":
-                    reasons.add(n)
-        if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+    def summary(self, t0: float, t1: float, busy=None):
+        """Median SM clock and the reasons seen in [t0, t1]; when that window
+        holds fewer than 3 samples, the busy window (t0', t1') around it
+        (warm-up, timed and profiled passes of the same work) is used and
+        named."""
+        def pick(a, b):
+            return [s for s in self.samples if a - 0.03 <= s[0] <= b + 0.03]
+        sel, window = pick(t0, t1), "timed"
+        if len(sel) < 3 and busy is not None:
+            sel, window = pick(*busy), "warm-up + timed + profiled passes of the same work"
+        if not sel:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0, "source": self.source}
+        reasons = sorted(set().union(*[s[4] for s in sel]))
+        return {"sm_mhz": statistics.median(s[1] for s in sel), "sm_max_mhz": max(s[2] for s in sel),
+                "power_w_max": round(max(s[3] for s in sel), 1), "reasons": reasons, "samples": len(sel),
+                "window": window, "source": self.source}
+
+
+def pci_bus_id(dev) -> str | None:
+    """NVML-style PCI bus id of a torch CUDA device, when torch reports it."""
+    import torch
+    p = torch.cuda.get_device_properties(dev)
+    if hasattr(p, "pci_bus_id") and hasattr(p, "pci_domain_id"):
+        return "%08X:%02X:%02X.0" % (p.pci_domain_id, p.pci_bus_id, getattr(p, "pci_device_id", 0))
+    return None
 
 
 TC_FLOPS_PER_DFT1024 = 2 * 12 * 128 * 64 * 16 * 2 / 4     # 2 stages x 12 MMAs (M128 N64 K16) per 4 transforms
@@ -289,29 +359,46 @@ def cpu_chain_rate(spec, kind: str, seconds: float = 10.0, max_blocks: int = 1 <
 
 
 # ---------------------------------------------------------------- GPU arm
-def run_gpu(args):
-    import torch
-    ws, rank = dist_init("nccl")
-    _, _, local = dist_env()
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    import psrdada_cpp_gb300 as G
-    from psrdada_cpp_gb300 import synth
+FORM_DTYPE = {"fp32": "f32", "bf16": "bf16 hi+lo, f32 accumulate", "fp16": "f16 hi+lo, f32 accumulate"}
 
-    spec, kind = workload(args.workload)
+
+def stokes_rel_err(got: np.ndarray, ref: np.ndarray, dual: bool, floor: float = 1e-2):
+    """Per-bin relative difference of two output records' spectra (Stokes
+    products normalised by I of the same bin), denominators floored at
+    ``floor`` x the spectrum's mean; returns (max, rms, per product max)."""
+    got = got.astype(np.float64)
+    ref = ref.astype(np.float64)
+    base = np.abs(ref[:, 0:1]) if dual else np.abs(ref)
+    denom = np.maximum(base, floor * base.mean(axis=-1, keepdims=True))
+    denom = np.where(denom == 0, 1.0, denom)
+    e = np.abs(got - ref) / denom
+    names = "IQUV" if dual else ("G0", "G1")
+    by = {n: float(e[:, i].max()) for i, n in enumerate(names)}
+    return float(e.max()), float(np.sqrt(np.mean(e * e))), by
+
+
+def record_spectra(buf: np.ndarray, n_out: int, C: int, dual: bool) -> np.ndarray:
+    rec = buf[:n_out * ((8 if dual else 2) * (4 * C + 8))].reshape(n_out, -1)
+    f = rec[:, :(8 if dual else 2) * 4 * C].copy().view("<f4")
+    return f.reshape(n_out, 4, 2, C) if dual else f.reshape(n_out, 2, C)
+
+
+def measure_form(args, form_name, spec, kind, host_blocks, d_blocks, dev, clocks):
+    """Times one arithmetic form of the chain on the workload: device
+    throughput (value), per-kernel roofline, end-to-end through the handler.
+    Returns the form's result dict and its first output block (host copy)."""
+    import torch
+    import psrdada_cpp_gb300 as G
+    ws, rank = dist_env()[0], dist_env()[1]
+    local = dev.index
+    form = {"fp32": G.FORM_FP32, "bf16": G.FORM_BF16, "fp16": G.FORM_FP16}[form_name]
     samples_per_step = spec.samples_per_pol * spec.npol
     lay = G.DadaBufferLayout(spec.buffer_size, spec.heap_size, spec.n_side_channels)
-    form = {"fp32": G.FORM_FP32, "bf16": G.FORM_BF16, "fp16": G.FORM_FP16}[args.form]
     mk = dict(input_type=G.DUAL_POL if spec.dual_pol else G.SINGLE_POL, device=local, form=form)
     gs = G.GatedSpectrometer(lay, 0, 0, spec.fft_length, spec.naccumulate, spec.nbits, 100.0, 100.0,
                              G.NullSink(), **mk)
     info = gs.info()
-    host_blocks = [synth.make_block(spec, seed=1 + rank, block_index=i, kind=kind) for i in range(2)]
-    # distinct device copies rotate so that one rotation is at least 3x the L2 size: every step
-    # reads its block from HBM, not from the previous step's L2 lines
-    l2_bytes = int(getattr(torch.cuda.get_device_properties(dev), "L2_cache_size", 0)) or L2_FALLBACK
-    nrot = max(2, -(-3 * l2_bytes // spec.buffer_size))
-    d_blocks = [torch.from_numpy(host_blocks[i % 2]).to(dev) for i in range(nrot)]
+    nrot = len(d_blocks)
     d_out = torch.zeros(int(info.output_bytes), dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
@@ -321,14 +408,17 @@ def run_gpu(args):
             d_out.zero_()
         gs.run_block_device(d_blocks[i % nrot].data_ptr(), d_out.data_ptr(), sptr)
 
+    # first output block from the zero baselines, kept for the form comparison
+    step(0)
+    torch.cuda.synchronize(dev)
+    first = d_out.cpu().numpy().copy()
+    gs.set_baselines(np.zeros(4, np.float32))
+    busy0 = time.time()
     for i in range(args.warmup):
         step(i)
     torch.cuda.synchronize(dev)
 
     # ---- device throughput (value)
-    clocks = ClockSampler(local)
-    clocks.start()
-    time.sleep(0.3)
     launches0 = gs.info().kernel_launches
     dist_barrier()
     torch.cuda.synchronize(dev)
@@ -342,14 +432,12 @@ def run_gpu(args):
     tw1 = time.time()
     dist_barrier()
     launches = gs.info().kernel_launches - launches0
-    clocks.stop()
     ms = ev0.elapsed_time(ev1)
     ms_max = dist_max(ms, dev)
     total_samples = dist_sum(samples_per_step * args.steps, dev)
     value = total_samples / (ms_max / 1e3) / 1e9
-    clk = clocks.summary(tw0, tw1)
 
-    # ---- per-kernel profile (roofline)
+    # ---- per-kernel profile (roofline): CUDA events on the chain's stream
     gs.reset_profile()
     gs.set_profiling(True)
     nprof = max(4, min(32, args.steps))
@@ -357,6 +445,9 @@ def run_gpu(args):
         step(i)
     prof = gs.profile()
     gs.set_profiling(False)
+    torch.cuda.synchronize(dev)
+    busy1 = time.time()
+    clk = clocks.summary(tw0, tw1, busy=(busy0, busy1))
     kernels = {k: v for k, v in prof.items() if v[1] > 0}
     tot_ms = sum(v[2] for v in kernels.values())
     dom = max(kernels, key=lambda k: kernels[k][2])
@@ -381,7 +472,7 @@ def run_gpu(args):
     roofline = {
         "bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
         "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} copy bandwidth",
-        "traffic": ncu_traffic(dom, spec.name if args.form == "fp32" else f"{spec.name}_{args.form}"),
+        "traffic": ncu_traffic(dom, spec.name if form_name == "fp32" else f"{spec.name}_{form_name}"),
         "algorithmic_bytes_per_launch": int(alg_bytes_launch), "mean_launch_ms": round(per_launch_ms, 4),
         "chain": {"ms_per_block": round(chain_ms, 4), "algorithmic_bytes_per_block": in_bytes + out_bytes,
                   "achieved_GBs": round(chain_gbs, 1), "frac": round(chain_gbs / peak, 4)},
@@ -392,21 +483,22 @@ def run_gpu(args):
                      "achieved_tflops": round(fft_flops / (chain_ms / 1e3) / 1e12, 2)},
         "tensor": tensor_roofline(spec, info, form, kernels, nprof, G),
     }
+    gs.close()
+    del d_out
 
     # ---- end to end through the handler API, pinned host blocks
-    e2e = None
-    lat = []
+    e2e, lat = None, []
     if not args.no_e2e:
         pinned = []
         for b in host_blocks:
             t = torch.empty(b.size, dtype=torch.uint8, pin_memory=True)
             t.numpy()[:] = b
             pinned.append(t)
-        sink = G.NullSink()
-        ge = G.GatedSpectrometer(lay, 0, 0, spec.fft_length, spec.naccumulate, spec.nbits, 100.0, 100.0, sink, **mk)
+        ge = G.GatedSpectrometer(lay, 0, 0, spec.fft_length, spec.naccumulate, spec.nbits, 100.0, 100.0,
+                                 G.NullSink(), **mk)
         raws = [G.RawBytes(p.numpy()) for p in pinned]
         for i in range(max(3, args.warmup)):
-            ge(raws[i % 2])
+            ge(raws[i % len(raws)])
         torch.cuda.synchronize(dev)
         ke = max(8, min(args.steps, 1000))
         dist_barrier()
@@ -414,7 +506,7 @@ def run_gpu(args):
         t0 = time.perf_counter()
         for i in range(ke):
             c0 = time.perf_counter()
-            ge(raws[i % 2])
+            ge(raws[i % len(raws)])
             lat.append((time.perf_counter() - c0) * 1e3)
         torch.cuda.synchronize(dev)
         t1 = time.perf_counter()
@@ -427,6 +519,44 @@ def run_gpu(args):
                "d2h_bytes_per_step": int(out_bytes * outputs_per_step), "steps": ke,
                "api": "GatedSpectrometer.__call__ -> gspec_process (pinned host blocks)"}
         ge.close()
+        del pinned, raws
+    res = {"value": round(value, 3), "ms_per_step": round(ms_max / args.steps, 4), "dtype": FORM_DTYPE[form_name],
+           "gpu_launches": int(launches), "clocks": clk, "roofline": roofline, "e2e": e2e,
+           "n1": int(info.n1), "n2": int(info.n2)}
+    if lat:
+        res["latency_ms"] = {"p50": round(float(np.percentile(lat, 50)), 3),
+                             "p95": round(float(np.percentile(lat, 95)), 3),
+                             "p99": round(float(np.percentile(lat, 99)), 3),
+                             "what": "host time of one handler call (H2D of the block, launch of the chain, "
+                                     "output D2H issue)"}
+    return res, first, info
+
+
+def run_gpu(args):
+    import torch
+    ws, rank = dist_init("nccl")
+    _, _, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from psrdada_cpp_gb300 import synth
+
+    spec, kind = workload(args.workload)
+    forms = [args.form] + ([] if args.form == "fp32" or args.no_compare else ["fp32"])
+    # two host blocks where they are cheap to make; one (used twice) at 2^28 samples/pol
+    nhost = 1 if spec.samples_per_pol >= (1 << 27) else 2
+    host_blocks = [synth.make_block(spec, seed=1 + rank, block_index=i, kind=kind) for i in range(nhost)]
+    # distinct device copies rotate so that one rotation is at least 3x the L2 size: every step
+    # reads its block from HBM, not from the previous step's L2 lines
+    l2_bytes = int(getattr(torch.cuda.get_device_properties(dev), "L2_cache_size", 0)) or L2_FALLBACK
+    nrot = max(2, -(-3 * l2_bytes // spec.buffer_size))
+    d_blocks = [torch.from_numpy(host_blocks[i % nhost]).to(dev) for i in range(nrot)]
+    clocks = ClockSampler(local, pci_bus_id(dev))
+    clocks.start()
+    results, firsts, info = {}, {}, None
+    for f in forms:
+        results[f], firsts[f], info = measure_form(args, f, spec, kind, host_blocks, d_blocks, dev, clocks)
+    clocks.stop()
+    del d_blocks
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -436,28 +566,46 @@ def run_gpu(args):
         except Exception as exc:  # the CPU leg never hides a GPU result
             cpu = {"value": None, "unit": UNIT, "cores": cpu_cores(), "kind": "port", "sample": f"failed: {exc}"}
 
-    gs.close()
     if rank == 0:
+        main = results[args.form]
+        if args.workload == "c3" and len(forms) > 1:
+            metric = METRIC
+        else:
+            metric = (f"input Gsamples/s gated {'Stokes' if spec.dual_pol else 'power'}, {args.form} form"
+                      + (" (fp32 form beside it)" if len(forms) > 1 else ""))
         line = {
-            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None,
-            "dtype": {"fp32": "f32", "bf16": "bf16 hi+lo, f32 accumulate", "fp16": "f16 hi+lo, f32 accumulate"}[args.form],
-            "data": "synthetic",
+            "metric": metric, "value": main["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": main["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": main["dtype"], "data": "synthetic",
             "config": {"workload": spec.name, "fft_length": spec.fft_length, "naccumulate": spec.naccumulate,
                        "nbits": spec.nbits, "pols": spec.npol, "samples_per_pol_per_block": spec.samples_per_pol,
-                       "block_bytes": spec.buffer_size, "form": args.form,
-                       "l2": "inputs larger than L2: %d device blocks of %d B rotate (L2 %d B)" % (nrot, spec.buffer_size, l2_bytes),
+                       "block_bytes": spec.buffer_size, "form": args.form, "n1": main["n1"], "n2": main["n2"],
+                       "diode_period_heaps": spec.diode_period_heaps,
+                       "l2": "inputs larger than L2: %d device blocks of %d B rotate (L2 %d B)"
+                             % (nrot, spec.buffer_size, l2_bytes),
                        "parallelism": f"replicas x{ws} (one independent stream per GPU)"},
-            "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "roofline": roofline,
-            "cpu_baseline": cpu,
+            "e2e": main["e2e"], "gpu_launches": main["gpu_launches"], "clocks": main["clocks"],
+            "roofline": main["roofline"], "cpu_baseline": cpu,
         }
-        if lat:
-            line["latency_ms"] = {"p50": round(float(np.percentile(lat, 50)), 3),
-                                  "p95": round(float(np.percentile(lat, 95)), 3),
-                                  "p99": round(float(np.percentile(lat, 99)), 3),
-                                  "what": "host time of one handler call (H2D of the block, launch of the chain, "
-                                          "output D2H issue)"}
+        if "latency_ms" in main:
+            line["latency_ms"] = main["latency_ms"]
+        if len(forms) > 1:
+            fp = results["fp32"]
+            line["forms"] = {f: {k: r[k] for k in ("value", "ms_per_step", "dtype", "e2e", "roofline", "clocks",
+                                                   "gpu_launches")} for f, r in results.items()}
+            line["tc_over_fp32"] = {"value": round(main["value"] / fp["value"], 4),
+                                    "e2e": (round(main["e2e"]["value"] / fp["e2e"]["value"], 4)
+                                            if main["e2e"] and fp["e2e"] else None),
+                                    "target": 3.0}
+            mx, rms, by = stokes_rel_err(
+                record_spectra(firsts[args.form], int(info.n_out), int(info.nchans), spec.dual_pol),
+                record_spectra(firsts["fp32"], int(info.n_out), int(info.nchans), spec.dual_pol),
+                spec.dual_pol)
+            line["tc_vs_fp32_spectra"] = {
+                "max_rel": mx, "rms_rel": rms, "by_product_max": by,
+                "what": "first output block of the same input through both forms; per-bin |diff| over I of the "
+                        "bin (floor 1 % of the mean I). The FP32 form is itself within 1e-5 of the FP64 oracle "
+                        "(GPU parity tests), so this bounds the tensor-core form's error to within 1e-5"}
         print(json.dumps(line), flush=True)
 
 
@@ -492,13 +640,13 @@ def run_batch(args):
     for i, h in enumerate(host):
         bt.set_input(i, h, sp)
     torch.cuda.synchronize(dev)
+    clocks = ClockSampler(local, pci_bus_id(dev))
+    clocks.start()
+    busy0 = time.time()
     for _ in range(args.warmup):
         bt.run(sp)
     torch.cuda.synchronize(dev)
     steps = args.steps
-    clocks = ClockSampler(local)
-    clocks.start()
-    time.sleep(0.3)
     dist_barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     tw0 = time.time()
@@ -509,7 +657,6 @@ def run_batch(args):
     torch.cuda.synchronize(dev)
     tw1 = time.time()
     dist_barrier()
-    clocks.stop()
     ms = dist_max(e0.elapsed_time(e1), dev)
     value = dist_sum(samples_per_step * steps, dev) / (ms / 1e3) / 1e9
     kernels = bt.kernels_per_step()
@@ -536,6 +683,8 @@ def run_batch(args):
             g.run_block_device(di.data_ptr(), do.data_ptr(), sp)
     e1.record(stream)
     torch.cuda.synchronize(dev)
+    busy1 = time.time()
+    clocks.stop()
     seq_value = samples_per_step * ks / (e0.elapsed_time(e1) / 1e3) / 1e9
     for g in seq:
         g.close()
@@ -598,7 +747,7 @@ def run_batch(args):
                     "api": "Batch.set_input (pinned, copy stream, one step ahead) -> gspec_batch_run -> "
                            "gspec_batch_copy_output (pinned)"},
             "gpu_launches": int(kernels * steps), "kernels_per_graph": int(kernels),
-            "clocks": clocks.summary(tw0, tw1),
+            "clocks": clocks.summary(tw0, tw1, busy=(busy0, busy1)),
         }
         print(json.dumps(line), flush=True)
 
@@ -639,7 +788,7 @@ def run_serve(args):
     peak = loadgen.run(specs, host, burst, budget, device=local, tunes=tunes, priorities=prios, inflight_bytes=infl)
     rate = 0.6 * peak["gsamples_per_s"] * 1e9 / len(specs)
     plan = loadgen.poisson_plan(specs, rate, args.serve_blocks, seed=4)
-    clocks = ClockSampler(local)
+    clocks = ClockSampler(local, pci_bus_id(torch.device("cuda", local)))
     clocks.start()
     tw0 = time.time()
     res = loadgen.run(specs, host, plan, budget, device=local, tunes=tunes, priorities=prios, inflight_bytes=infl)
@@ -724,10 +873,14 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["c1", "c2", "c3", "c4", "c5"], default="c2",
-                    help="c1-c3 one stream; c4 16 uneven streams in one CUDA graph; c5 the serving loop")
-    ap.add_argument("--form", choices=["fp32", "bf16", "fp16"], default="fp32",
-                    help="FFT arithmetic: FP32 CUDA cores, or tensor-core DFT-32 stages with BF16/FP16 hi+lo halves")
+    ap.add_argument("--workload", choices=["c1", "c2", "c2m", "c3", "c4", "c5"], default="c3",
+                    help="c1-c3 one stream (c2m: c2 with a 61-heap diode period); c4 16 uneven streams in one "
+                         "CUDA graph; c5 the serving loop")
+    ap.add_argument("--form", choices=["fp32", "bf16", "fp16"], default=None,
+                    help="FFT arithmetic: FP32 CUDA cores, or tensor-core DFT-32 stages with BF16/FP16 hi+lo "
+                         "halves (default: bf16 for c3, fp32 otherwise)")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="time only --form (by default a tensor-core form is timed beside the FP32 form)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="wall seconds of the timed CPU sample")
@@ -741,6 +894,8 @@ def main(argv=None):
                     help="c5: fft-2^20 blocks on the GPU at once over all streams (0: no limit)")
     ap.add_argument("--connections", type=int, default=32, help="c5: CUDA_DEVICE_MAX_CONNECTIONS")
     args = ap.parse_args(argv)
+    if args.form is None:
+        args.form = "bf16" if args.workload == "c3" else "fp32"
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -187,9 +187,14 @@ int gspec_get_saturation(gspec_handle* h, uint64_t* out);
  * memory is a library-owned device array of GSPEC_NOALLOC_SCRATCH_BYTES held
  * by every GPU that loads the library.  Only fft_length <= 4096; larger
  * working sets are rejected (GSPEC_ERR_UNSUPPORTED) with the reason in err.
- * cfg->device must be the current device; the first call on a device looks
- * up the array's device address and should come before any stream capture.
- * All calls share the array: calls that overlap on the GPU race. */
+ * cfg->device must be the current device.  The first call on a device looks
+ * up the array's device address; with CUDA's default lazy module loading that
+ * is also when the driver reserves the array's 32 MiB on that device, so make
+ * the first call at start-up, before the caller reserves the rest of the
+ * device memory for its pool and before any stream capture.  The address is
+ * kept per device number: it is valid for the primary context and is not
+ * looked up again after a cudaDeviceReset.  All calls share the array and it
+ * keeps the last call's contents: calls that overlap on the GPU race. */
 #define GSPEC_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 int gspec_process_block_noalloc(const gspec_config* cfg, const void* d_block, float* d_baselines, void* d_out,
                                 void* cuda_stream, char* err, size_t err_len);

@@ -435,6 +435,81 @@ def process_block(block: np.ndarray, cfg: Config, states: list, period_counts=(0
     return BlockResult(spectra, n0, n1, sat0, sat1, gated, pol_counts, pol_sums)
 
 
+def _item_index_range(cfg: Config, s0: int, s1: int) -> np.ndarray:
+    """:func:`sample_item_index` for pol samples ``[s0, s1)`` only."""
+    s = np.arange(s0, s1, dtype=np.int64)
+    nsc, sel = cfg.layout.n_side_channels, cfg.selected_side_channel
+    if cfg.convention == "reference":
+        L = cfg.chunk_len
+        j, t = s // L, s % L
+        return j * cfg.step + (t // cfg.layout.heap_size) * nsc + sel
+    return ((s * cfg.nbits) // (8 * cfg.layout.heap_size)) * nsc + sel
+
+
+def process_block_chunked(block: np.ndarray, cfg: Config, states: list, period_counts=(0, 0),
+                          outputs_per_chunk: int = 1) -> BlockResult:
+    """:func:`process_block` evaluated ``outputs_per_chunk`` output spectra
+    at a time, so that a full-size block (2^28 samples per pol) fits in a
+    few GB of host memory.  Same arithmetic, same FP64 FFT, same baseline
+    update (after both pols, ``edd/detail/GatedSpectrometer.cu:263-271``):
+    every quantity of the chain is a sum over samples of one output spectrum
+    or an exact integer sum over the block, so the chunking changes no
+    value."""
+    raws, items = split_block(block, cfg)
+    if cfg.dual_pol:
+        items = list(merge_side_channels(items[0], items[1], cfg.convention))
+    N, C, n_out, nacc = cfg.fft_length, cfg.nchans, cfg.n_out, cfg.nacc_per_block
+    L = cfg.chunk_len
+    lo, hi = -(1 << (cfg.nbits - 1)), (1 << (cfg.nbits - 1)) - 1
+    npol = len(raws)
+    n0 = np.zeros(n_out, np.uint64)
+    n1 = np.zeros(n_out, np.uint64)
+    sat0 = np.zeros(n_out, np.uint64)
+    sat1 = np.zeros(n_out, np.uint64)
+    spectra = np.zeros((n_out, 4, 2, C)) if cfg.dual_pol else np.zeros((n_out, 2, C))
+    tot = [[0, 0] for _ in range(npol)]
+    sums = [[0, 0] for _ in range(npol)]
+    b = [(np.float32(st.b0), np.float32(st.b1)) for st in states]
+    for k0 in range(0, n_out, outputs_per_chunk):
+        k1 = min(n_out, k0 + outputs_per_chunk)
+        s0, s1 = k0 * L, k1 * L
+        idx = _item_index_range(cfg, s0, s1)
+        X = []
+        for p in range(npol):
+            raw = raws[p][s0 * cfg.nbits // 8:s1 * cfg.nbits // 8]
+            v = unpack(raw, cfg.nbits)
+            g0, g1, m0, m1 = gate(v, items[p][idx], cfg.selected_bit, b[p][0], b[p][1])
+            c0 = m0.reshape(k1 - k0, L).sum(axis=1).astype(np.uint64)
+            c1 = m1.reshape(k1 - k0, L).sum(axis=1).astype(np.uint64)
+            sat = (v == lo) | (v == hi)
+            sat0[k0:k1] += (sat & m0).reshape(k1 - k0, L).sum(axis=1).astype(np.uint64)
+            sat1[k0:k1] += (sat & m1).reshape(k1 - k0, L).sum(axis=1).astype(np.uint64)
+            n0[k0:k1] += c0
+            n1[k0:k1] += c1
+            tot[p][0] += int(c0.sum())
+            tot[p][1] += int(c1.sum())
+            sums[p][0] += int(np.sum(v.astype(np.int64) * m0))
+            sums[p][1] += int(np.sum(v.astype(np.int64) * m1))
+            X.append((rfft64(g0.reshape(-1, N)), rfft64(g1.reshape(-1, N))))
+        if not cfg.dual_pol:
+            for g in range(2):
+                spectra[k0:k1, g] = (np.abs(X[0][g]) ** 2).reshape(k1 - k0, nacc, C).sum(axis=1)
+        else:
+            for g in range(2):
+                for si, S in enumerate(stokes_iquv(X[0][g], X[1][g])):
+                    spectra[k0:k1, si, g] = S.reshape(k1 - k0, nacc, C).sum(axis=1)
+    cum0, cum1 = period_counts
+    for p in range(npol):
+        st = states[p]
+        if cfg.convention == "reference":
+            cum0 += tot[p][0]
+            cum1 += tot[p][1]
+            st.b0, st.b1 = baseline(sums[p][0], cum0), baseline(sums[p][1], cum1)
+        else:
+            st.b0, st.b1 = baseline(sums[p][0], tot[p][0]), baseline(sums[p][1], tot[p][1])
+    return BlockResult(spectra, n0, n1, sat0, sat1, [], [tuple(t) for t in tot], [tuple(s) for s in sums])
+
+
 # --------------------------------------------------------------------------
 # R13 / R14: output block layout
 # --------------------------------------------------------------------------

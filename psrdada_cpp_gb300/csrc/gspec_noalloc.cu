@@ -20,7 +20,12 @@
 // code it names a host-side stand-in), so the first call on each device, with
 // that device current, asks the runtime for the device address with
 // cudaGetSymbolAddress and keeps it; that first call should therefore come
-// before any stream capture.  All calls share the one array and it keeps the
+// before any stream capture.  Under CUDA's default lazy module loading the
+// driver also reserves the array on the device at that first lookup, so a
+// caller that reserves all remaining device memory for its own pool makes the
+// first call at start-up, before reserving it.  The kept address belongs to
+// the device's primary context; it is not refreshed after a cudaDeviceReset.
+// All calls share the one array and it keeps the
 // last call's contents: the per-pol statistics and saturation counts are
 // cleared by every call, everything else is fully rewritten.  Calls whose
 // work overlaps on the GPU (different streams, or different host threads)

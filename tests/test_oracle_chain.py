@@ -175,3 +175,29 @@ def test_synth_diode_and_lost():
     state = (it[:, 1] >> np.uint64(5)) & np.uint64(1)
     assert list(state[:4]) == [0, 0, 1, 1]
     assert ((it[:, 1] >> np.uint64(63)) != 0).any()
+
+
+@pytest.mark.parametrize("name,spec,convention", [
+    ("s8", synth.StreamSpec("ck_s8", 8, False, 4096, 1, 1 << 15, 512, 8, diode_period_heaps=3), "intended"),
+    ("s8_ref", synth.StreamSpec("ck_s8r", 8, False, 4096, 1, 1 << 15, 512, 8, diode_period_heaps=3), "reference"),
+    ("d12", synth.StreamSpec("ck_d12", 12, True, 6144, 1, 1 << 15, 1024, 4, diode_period_heaps=1), "intended"),
+    ("d10_ref", synth.StreamSpec("ck_d10", 10, True, 5120, 1, 1 << 15, 512, 8, diode_period_heaps=2),
+     "intended"),
+])
+def test_chunked_oracle_equals_whole_block(name, spec, convention):
+    """The output-chunked evaluation used for full-size blocks gives the same
+    spectra, counters and next-block baselines as the whole-block one."""
+    cfg = cfg_of(spec, convention)
+    start = [O.PolState(np.float32(1.5), np.float32(-2.25)) for _ in range(spec.npol)]
+    for b in range(2):
+        blk = synth.make_block(spec, seed=9, block_index=b, lost_frac=0.1, extra_bits=True)
+        sa = [O.PolState(s.b0, s.b1) for s in start]
+        sb = [O.PolState(s.b0, s.b1) for s in start]
+        ra = O.process_block(blk, cfg, sa, period_counts=(3, 5))
+        rb = O.process_block_chunked(blk, cfg, sb, period_counts=(3, 5), outputs_per_chunk=3)
+        assert np.allclose(ra.spectra, rb.spectra, rtol=1e-12, atol=1e-9)
+        for f in ("n0", "n1", "sat0", "sat1"):
+            assert np.array_equal(getattr(ra, f), getattr(rb, f)), f
+        assert ra.pol_counts == rb.pol_counts and ra.pol_sums == rb.pol_sums
+        assert [(s.b0, s.b1) for s in sa] == [(s.b0, s.b1) for s in sb]
+        start = sa
