@@ -91,8 +91,14 @@ struct GatedFullStokesOutput {
 template <class HandlerType, class InputType, class OutputType, class RawBytesType = RawBytes>
 class GatedSpectrometer {
  public:
-  // edd/GatedSpectrometer.cuh:292-297
-  GatedSpectrometer(const DadaBufferLayout& bufferLayout, std::size_t selectedSideChannel, std::size_t selectedBit,
+  // edd/GatedSpectrometer.cuh:292-297.  The layout is any type with the
+  // getters of psrdada_cpp::effelsberg::edd::DadaBufferLayout
+  // (edd/DadaBufferLayout.hpp:31-51: getBufferSize, getHeapSize,
+  // getNSideChannels), so the reference's own layout, constructed from a ring
+  // buffer key, passes unchanged; DadaBufferLayout above is the stand-alone
+  // equivalent.
+  template <class LayoutType>
+  GatedSpectrometer(const LayoutType& bufferLayout, std::size_t selectedSideChannel, std::size_t selectedBit,
                     std::size_t fft_length, std::size_t naccumulate, std::size_t nbits, float input_level,
                     float output_level, HandlerType& handler, uint32_t convention = GSPEC_INTENDED,
                     int device = 0, uint32_t flags = 0)

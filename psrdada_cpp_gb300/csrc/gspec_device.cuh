@@ -407,6 +407,18 @@ struct GateStats {
   long long s0 = 0, s1 = 0;
 };
 
+// Exact sum of one gated sequence's in-gate values (the four-step path's
+// DC bins): s = sum of the integer samples, n = their count, r = the sum of
+// the rounding residues (v - b) + b - v of the reference's gate formula.  A
+// residue is the difference of a float and the integer sample (|v| <= 2048)
+// it rounds to within one ulp, so it is a multiple of 2^-24 of at most 2^-12
+// in magnitude: a thread's sum of at most 128 of them is exact in FP32.  The
+// out-of-gate samples are the baseline; the reader adds (N - n) * b.
+struct DcAcc {
+  int s = 0, n = 0;
+  float r = 0.f;
+};
+
 // Gate masks of an item index from the mask pass.
 __device__ __forceinline__ void mask_of(const GateParams& g, uint32_t idx, bool& m0, bool& m1) {
   const uint32_t m = __ldg(g.masks + idx);
@@ -421,7 +433,8 @@ __device__ __forceinline__ void mask_of(const GateParams& g, uint32_t idx, bool&
 template <int NBITS, int GS = Group<NBITS>::samples>
 __device__ __forceinline__ void gate_group(const GateParams& g, int pol, uint32_t s, float b0, float b1,
                                            float (&g0)[GS], float (&g1)[GS],
-                                           GateStats& st, uint32_t stat_gates = 3u) {
+                                           GateStats& st, uint32_t stat_gates = 3u, DcAcc* dc0 = nullptr,
+                                           DcAcc* dc1 = nullptr) {
   int v[GS];
   const uint64_t byte0 = static_cast<uint64_t>(s) * NBITS / 8;
   unpack_span<NBITS, GS>(pol_byte(g, pol, byte0), v);
@@ -442,11 +455,16 @@ __device__ __forceinline__ void gate_group(const GateParams& g, int pol, uint32_
   if (ib == ia) {
     // the whole group lies in one heap: statistics per group
     int sumv = 0, satc = 0;
+    float r0 = 0.f, r1 = 0.f;
 #pragma unroll
     for (int i = 0; i < GS; ++i) {
       const float vf = static_cast<float>(v[i]);
       g0[i] = gate_value(vf, b0, a0);
       g1[i] = gate_value(vf, b1, a1);
+      if (dc0) {
+        r0 += g0[i] - vf;
+        r1 += g1[i] - vf;
+      }
       sumv += v[i];
       satc += (v[i] == lo) | (v[i] == hi);
     }
@@ -454,11 +472,21 @@ __device__ __forceinline__ void gate_group(const GateParams& g, int pol, uint32_
       st.n0 += GS;
       st.s0 += sumv;
       st.sat0 += satc;
+      if (dc0) {
+        dc0->s += sumv;
+        dc0->n += GS;
+        dc0->r += r0;
+      }
     }
     if (a1 && k1) {
       st.n1 += GS;
       st.s1 += sumv;
       st.sat1 += satc;
+      if (dc1) {
+        dc1->s += sumv;
+        dc1->n += GS;
+        dc1->r += r1;
+      }
     }
     return;
   }
@@ -478,6 +506,16 @@ __device__ __forceinline__ void gate_group(const GateParams& g, int pol, uint32_
     st.sat1 += (q1 && sat);
     st.s0 += q0 ? v[i] : 0;
     st.s1 += q1 ? v[i] : 0;
+    if (dc0 && q0) {
+      dc0->s += v[i];
+      dc0->n += 1;
+      dc0->r += g0[i] - vf;
+    }
+    if (dc1 && q1) {
+      dc1->s += v[i];
+      dc1->n += 1;
+      dc1->r += g1[i] - vf;
+    }
   }
 }
 
@@ -485,7 +523,7 @@ __device__ __forceinline__ void gate_group(const GateParams& g, int pol, uint32_
 // that gate only when `stats` is set.
 template <int NBITS, int GS = Group<NBITS>::samples>
 __device__ __forceinline__ void gate_group1(const GateParams& g, int pol, uint32_t s, float b, int gate,
-                                            float (&out)[GS], GateStats& st, bool stats) {
+                                            float (&out)[GS], GateStats& st, bool stats, DcAcc* dc = nullptr) {
   int v[GS];
   const uint64_t byte0 = static_cast<uint64_t>(s) * NBITS / 8;
   unpack_span<NBITS, GS>(pol_byte(g, pol, byte0), v);
@@ -495,10 +533,13 @@ __device__ __forceinline__ void gate_group1(const GateParams& g, int pol, uint32
   const bool ma = (__ldg(g.masks + ia) >> sh) & 1u;
   constexpr int lo = -(1 << (NBITS - 1)), hi = (1 << (NBITS - 1)) - 1;
   int sumv = 0, satc = 0, cnt = 0;
+  float res = 0.f;
   if (ib == ia) {
 #pragma unroll
     for (int i = 0; i < GS; ++i) {
-      out[i] = gate_value(static_cast<float>(v[i]), b, ma);
+      const float vf = static_cast<float>(v[i]);
+      out[i] = gate_value(vf, b, ma);
+      if (dc) res += out[i] - vf;
       sumv += v[i];
       satc += (v[i] == lo) | (v[i] == hi);
     }
@@ -511,7 +552,9 @@ __device__ __forceinline__ void gate_group1(const GateParams& g, int pol, uint32
 #pragma unroll
     for (int i = 0; i < GS; ++i) {
       const bool m = (s + i) >= boundary ? mb : ma;
-      out[i] = gate_value(static_cast<float>(v[i]), b, m);
+      const float vf = static_cast<float>(v[i]);
+      out[i] = gate_value(vf, b, m);
+      if (dc && m) res += out[i] - vf;
       cnt += m;
       sumv += m ? v[i] : 0;
       satc += m && ((v[i] == lo) | (v[i] == hi));
@@ -527,6 +570,11 @@ __device__ __forceinline__ void gate_group1(const GateParams& g, int pol, uint32
       st.s0 += sumv;
       st.sat0 += satc;
     }
+    if (dc && cnt) {
+      dc->s += sumv;
+      dc->n += cnt;
+      dc->r += res;
+    }
   }
 }
 
@@ -537,7 +585,7 @@ __device__ __forceinline__ void gate_group1(const GateParams& g, int pol, uint32
 template <int NBITS, int GS = Group<NBITS>::samples>
 __device__ __forceinline__ void gate_group_dual(const GateParams& g, uint32_t s, float b0, float b1, int gate,
                                                 float (&re)[GS], float (&im)[GS], GateStats& st0, GateStats& st1,
-                                                bool stats) {
+                                                bool stats, DcAcc* dc0 = nullptr, DcAcc* dc1 = nullptr) {
   const uint32_t byte0 = static_cast<uint32_t>(static_cast<uint64_t>(s) * NBITS / 8);
   const uint32_t h = heap_of(g, byte0);
   const uint8_t* p0 = g.block + 2ull * h * g.heap_size + (byte0 - h * g.heap_size);
@@ -550,11 +598,17 @@ __device__ __forceinline__ void gate_group_dual(const GateParams& g, uint32_t s,
   const bool ma = (__ldg(g.masks + ia) >> sh) & 1u;
   constexpr int lo = -(1 << (NBITS - 1)), hi = (1 << (NBITS - 1)) - 1;
   int sum0 = 0, sum1 = 0, sat0 = 0, sat1 = 0, cnt = 0;
+  float r0 = 0.f, r1 = 0.f;
   if (ib == ia) {
 #pragma unroll
     for (int i = 0; i < GS; ++i) {
-      re[i] = gate_value(static_cast<float>(v0[i]), b0, ma);
-      im[i] = gate_value(static_cast<float>(v1[i]), b1, ma);
+      const float f0 = static_cast<float>(v0[i]), f1 = static_cast<float>(v1[i]);
+      re[i] = gate_value(f0, b0, ma);
+      im[i] = gate_value(f1, b1, ma);
+      if (dc0) {
+        r0 += re[i] - f0;
+        r1 += im[i] - f1;
+      }
       sum0 += v0[i];
       sum1 += v1[i];
       sat0 += (v0[i] == lo) | (v0[i] == hi);
@@ -569,14 +623,27 @@ __device__ __forceinline__ void gate_group_dual(const GateParams& g, uint32_t s,
 #pragma unroll
     for (int i = 0; i < GS; ++i) {
       const bool m = (s + i) >= boundary ? mb : ma;
-      re[i] = gate_value(static_cast<float>(v0[i]), b0, m);
-      im[i] = gate_value(static_cast<float>(v1[i]), b1, m);
+      const float f0 = static_cast<float>(v0[i]), f1 = static_cast<float>(v1[i]);
+      re[i] = gate_value(f0, b0, m);
+      im[i] = gate_value(f1, b1, m);
+      if (dc0 && m) {
+        r0 += re[i] - f0;
+        r1 += im[i] - f1;
+      }
       cnt += m;
       sum0 += m ? v0[i] : 0;
       sum1 += m ? v1[i] : 0;
       sat0 += m && ((v0[i] == lo) | (v0[i] == hi));
       sat1 += m && ((v1[i] == lo) | (v1[i] == hi));
     }
+  }
+  if (dc0 && stats && cnt) {
+    dc0->s += sum0;
+    dc0->n += cnt;
+    dc0->r += r0;
+    dc1->s += sum1;
+    dc1->n += cnt;
+    dc1->r += r1;
   }
   if (stats) {
     if (gate) {

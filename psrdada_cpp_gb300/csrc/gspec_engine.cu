@@ -271,6 +271,7 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
     f.jobs = h->d_jobs;
     f.njobs = h->d_njobs;
     f.dc = h->d_dc;
+    f.dcsum = h->d_dcsum;
     // job lists of every output spectrum of the block
     f.k0 = 0;
     f.nk = static_cast<uint32_t>(h->n_out);
@@ -320,7 +321,8 @@ void release(gspec_handle* h) {
   }
   void* ptrs[] = {h->d_sat_dev, h->d_baselines, h->d_pol_stats, h->d_tw,   h->d_tw1,   h->d_tw2,  h->d_twA,
                   h->d_twB,     h->d_partial,   h->d_scratch,   h->d_masks, h->d_flags, h->d_jobs, h->d_njobs,
-                  h->d_dc,      h->d_err,       h->d_tc_hi,     h->d_tc_lo, h->d_tc_w, h->d_tc_img, h->d_bsum};
+                  h->d_dc,      h->d_err,       h->d_tc_hi,     h->d_tc_lo, h->d_tc_w, h->d_tc_img, h->d_bsum,
+                  h->d_dcsum};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->h_err) cudaFreeHost(h->h_err);
@@ -501,7 +503,7 @@ uint64_t footprint(const gspec_handle* h) {
     t += 2 * sz(1024 * sizeof(float2));
     t += sz(static_cast<uint64_t>(h->kchunk) * h->maxjobs * N * sizeof(float2));
     t += sz(h->n_out * h->maxjobs * sizeof(uint32_t)) + sz(h->n_out * sizeof(uint32_t)) +
-         sz(2ull * h->n_out * sizeof(uint32_t));
+         sz(2ull * h->n_out * sizeof(uint32_t)) + sz(6ull * h->n_out * h->maxjobs * sizeof(unsigned long long));
     t += sz(bsum_bytes(h));
     if (h->cfg.form != GSPEC_FORM_FP32)
       t += 2 * sz(4096 * sizeof(uint16_t)) + sz(1024 * sizeof(float2)) + sz(tc::kImageBytesHost);
@@ -624,6 +626,7 @@ gspec_handle* gspec_create(const gspec_config* cfg, char* err, size_t err_len) {
         !dalloc(h, &h->d_jobs, h->n_out * h->maxjobs * sizeof(uint32_t), "job lists") ||
         !dalloc(h, &h->d_njobs, h->n_out * sizeof(uint32_t), "job counts") ||
         !dalloc(h, &h->d_dc, 2ull * h->n_out * sizeof(uint32_t), "dc counts") ||
+        !dalloc(h, &h->d_dcsum, 6ull * h->n_out * h->maxjobs * sizeof(unsigned long long), "dc sums") ||
         !dalloc(h, &h->d_bsum, gspec_engine::bsum_bytes(h), "pass-B sums"))
       return bail("");
     if (cfg->form != GSPEC_FORM_FP32) {

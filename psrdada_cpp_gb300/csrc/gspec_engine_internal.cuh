@@ -49,6 +49,7 @@ struct gspec_handle {
   uint32_t* d_jobs = nullptr;      // four-step job lists [kchunk][maxjobs]
   uint32_t* d_njobs = nullptr;
   uint32_t* d_dc = nullptr;
+  unsigned long long* d_dcsum = nullptr;   // four-step: exact DC sums per job
   uint16_t* d_tc_hi = nullptr;     // tensor-core form: DFT-32 operand halves
   uint16_t* d_tc_lo = nullptr;
   float2* d_tc_w = nullptr;        // W1024 twiddles

@@ -25,6 +25,7 @@ __global__ void fourstep_plan_kernel(FourStepParams p, int dual) {
   const uint32_t kk = blockIdx.x * blockDim.x + threadIdx.x;
   if (kk >= p.nk) return;
   const uint32_t k = p.k0 + kk;
+  for (uint32_t i = 0; i < 6 * p.maxjobs; ++i) p.dcsum[static_cast<size_t>(k) * p.maxjobs * 6 + i] = 0ull;
   uint32_t dc[2];
   p.njobs[k] = build_jobs(p.c.flags + k * p.c.nacc, p.c.nacc, dual != 0, p.jobs + k * p.maxjobs, dc);
   p.dc[2 * k] = dc[0];
@@ -88,6 +89,7 @@ __device__ __forceinline__ void fourstep_a_body(const FourStepParams& p) {
   static_assert((N1 * GPR + Cfg::THREADS - 1) / Cfg::THREADS * SP <= 128 && Cfg::THREADS <= 512,
                 "per-thread gate statistics fit the 32-bit commit");
   GateStats st[NPOL];
+  DcAcc dc[2];
   for (int w = tid; w < N1 * GPR; w += Cfg::THREADS) {
     const int n1 = w % N1;
     const int gi = w / N1;
@@ -96,13 +98,13 @@ __device__ __forceinline__ void fourstep_a_body(const FourStepParams& p) {
     float re[SP], im[SP];
     if constexpr (DUAL) {
       gate_group_dual<NBITS, SP>(p.c.g, frA * N + off, bl[ga], bl[2 + ga], ga, re, im, st[0], st[NPOL - 1],
-                                 count_stats);
+                                 count_stats, &dc[0], &dc[1]);
     } else if (fb == fa) {
-      gate_group<NBITS, SP>(p.c.g, 0, frA * N + off, bl[0], bl[1], re, im, st[0], sg_a);
+      gate_group<NBITS, SP>(p.c.g, 0, frA * N + off, bl[0], bl[1], re, im, st[0], sg_a, &dc[0], &dc[1]);
     } else {
-      gate_group1<NBITS, SP>(p.c.g, 0, frA * N + off, bl[ga], ga, re, st[0], count_stats);
+      gate_group1<NBITS, SP>(p.c.g, 0, frA * N + off, bl[ga], ga, re, st[0], count_stats, &dc[0]);
       if (fb != kNoFrame) {
-        gate_group1<NBITS, SP>(p.c.g, 0, frB * N + off, bl[gb], gb, im, st[0], count_stats);
+        gate_group1<NBITS, SP>(p.c.g, 0, frB * N + off, bl[gb], gb, im, st[0], count_stats, &dc[1]);
       } else {
 #pragma unroll
         for (int e = 0; e < SP; ++e) im[e] = 0.f;
@@ -141,11 +143,18 @@ __device__ __forceinline__ void fourstep_a_body(const FourStepParams& p) {
       dst[static_cast<size_t>(k1) * N2 + n2] = cmul(v, W);
     }
   }
-  commit_stats<NPOL>(p.c, st, k, (DUAL ? 8 : 2) * static_cast<int>(N / 2 + 1), red);
+  commit_stats<NPOL>(p.c, st, k, (DUAL ? 8 : 2) * static_cast<int>(N / 2 + 1), red, dc,
+                     p.dcsum + (static_cast<size_t>(k) * p.maxjobs + j) * 6);
 }
 
+// Columns of up to 256 points (at most 256 threads) are held to 64 registers
+// so that 65536 / (THREADS * 64) CTAs share an SM (4 at 256 points).
+template <int N1>
+constexpr int pass_a_min_blocks() {
+  return PassACfg<N1>::THREADS <= 256 ? 65536 / (PassACfg<N1>::THREADS * 64) : 1;
+}
 template <int N1, int NBITS, bool DUAL>
-__global__ void __launch_bounds__(PassACfg<N1>::THREADS) fourstep_a_kernel(FourStepParams p) {
+__global__ void __launch_bounds__(PassACfg<N1>::THREADS, pass_a_min_blocks<N1>()) fourstep_a_kernel(FourStepParams p) {
   fourstep_a_body<N1, NBITS, DUAL>(p);
 }
 
@@ -296,8 +305,9 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, GSPEC_PASSB_MINB)
       pair_slot<N2>(rp, a, r, k2, pr, k2p);
       for (int qq = 0; qq < nq; ++qq) {
         const uint32_t job = jw[qq];
-        const float2 za = work[(2 * qq + r) * Cfg::STRIDE + spad(k2)];
-        const float2 zb = work[(2 * qq + pr) * Cfg::STRIDE + spad(k2p)];
+        float2 za = work[(2 * qq + r) * Cfg::STRIDE + spad(k2)];
+        float2 zb = work[(2 * qq + pr) * Cfg::STRIDE + spad(k2p)];
+        if (rp == 0 && a == 0) za = zb = exact_dc(p, k, j0 + qq, job, DUAL);
         const uint32_t ga = job_ga(job);
         if constexpr (!DUAL) {
           const float sx = za.x + zb.x, sy = za.y - zb.y;

@@ -12,10 +12,17 @@ namespace gspec {
 // (|sample| <= 2048, so |sum| <= 2^18), and a CTA has at most 512 threads:
 // its counts and sums fit in 32 bits and each warp reduces them with one
 // redux.sync per value.
+//
+// With dc_out (the job's 6 DC slots), the CTA's exact DC sums of the job's two
+// packed sequences (dc[0] the real part, dc[1] the imaginary part) go to
+// dc_out[0..2] and dc_out[3..5] (sum, count, residue in units of 2^-24) the
+// same way: a thread's residue sum is a multiple of 2^-24 below 2^-5, so
+// r * 2^24 is an exact 32-bit integer and a CTA's total stays below 2^28.
 template <int NPOL>
 __device__ void commit_stats(const ChainParams& p, const GateStats (&st)[NPOL], uint32_t k, int vals_c,
-                       unsigned long long* red) {
-  constexpr int NV = 4 * NPOL + 4;
+                       unsigned long long* red, const DcAcc* dc = nullptr, unsigned long long* dc_out = nullptr) {
+  constexpr int NS = 4 * NPOL + 4;
+  constexpr int NV = NS + 6;
   int v[NV];
   uint32_t n0 = 0, n1 = 0, s0 = 0, s1 = 0;
 #pragma unroll
@@ -33,19 +40,30 @@ __device__ void commit_stats(const ChainParams& p, const GateStats (&st)[NPOL], 
   v[4 * NPOL + 1] = static_cast<int>(n1);
   v[4 * NPOL + 2] = static_cast<int>(s0);
   v[4 * NPOL + 3] = static_cast<int>(s1);
+  v[NS + 0] = dc ? dc[0].s : 0;
+  v[NS + 1] = dc ? dc[0].n : 0;
+  v[NS + 2] = dc ? __float2int_rn(dc[0].r * 0x1p24f) : 0;
+  v[NS + 3] = dc ? dc[1].s : 0;
+  v[NS + 4] = dc ? dc[1].n : 0;
+  v[NS + 5] = dc ? __float2int_rn(dc[1].r * 0x1p24f) : 0;
+  const int nv = dc_out ? NV : NS;
   int* red32 = reinterpret_cast<int*>(red);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
   for (int i = 0; i < NV; ++i) {
+    if (i >= nv) break;
     const int s = __reduce_add_sync(0xffffffffu, v[i]);
     if (lane == 0) red32[warp * NV + i] = s;
   }
   __syncthreads();
-  if (threadIdx.x < NV) {
+  if (threadIdx.x < nv) {
     long long tot = 0;
     for (int w = 0; w < nw; ++w) tot += red32[w * NV + threadIdx.x];
     const int i = threadIdx.x;
-    if (tot) {
+    if (tot && i >= NS) {
+      // DC sums of the job: [0..2] the real part, [3..5] the imaginary part
+      atomicAdd(dc_out + (i - NS), static_cast<unsigned long long>(tot));
+    } else if (tot) {
       const unsigned long long u = static_cast<unsigned long long>(tot);
       if (i < 4 * NPOL) {
         atomicAdd(p.pol_stats + i, u);
@@ -77,6 +95,28 @@ __device__ __forceinline__ void pair_slot(uint32_t rp, int a, int& r, int& k2, i
     if (a <= N2 / 2) { r = 0; k2 = a; pr = 0; k2p = (N2 - a) & (N2 - 1); }
     else { r = 1; k2 = a - N2 / 2 - 1; pr = 1; k2p = N2 - 1 - k2; }
   }
+}
+
+// Bin 0 of job j of output spectrum k, computed exactly: the real and the
+// imaginary packed sequence each sum to (integer in-gate sum) + (residues) +
+// (N - in-gate count) * baseline, evaluated in FP64 and rounded once.  An FP32
+// FFT forms bin 0 by adding the integer samples and the fractional baseline
+// fill in FP32, which rounds with a systematic bias (~1e-5 of the bin at
+// 2^20 points); every other bin's rounding is unbiased.
+__device__ __forceinline__ float2 exact_dc(const FourStepParams& p, uint32_t k, uint32_t j, uint32_t job,
+                                           bool dual) {
+  const long long* d = reinterpret_cast<const long long*>(p.dcsum) + (static_cast<size_t>(k) * p.maxjobs + j) * 6;
+  const double n = static_cast<double>(p.N1) * static_cast<double>(p.N2);
+  const uint32_t ga = job_ga(job);
+  const double b_re = p.c.baselines[ga];
+  const double b_im = dual ? p.c.baselines[2 + ga] : p.c.baselines[job_gb(job)];
+  const double re = static_cast<double>(d[0]) + static_cast<double>(d[2]) * 0x1p-24 +
+                    (n - static_cast<double>(d[1])) * b_re;
+  const double im = (!dual && job_fb(job) == kNoFrame)
+                        ? 0.0
+                        : static_cast<double>(d[3]) + static_cast<double>(d[5]) * 0x1p-24 +
+                              (n - static_cast<double>(d[4])) * b_im;
+  return make_float2(static_cast<float>(re), static_cast<float>(im));
 }
 
 }  // namespace gspec

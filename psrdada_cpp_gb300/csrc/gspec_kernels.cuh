@@ -45,6 +45,7 @@ struct FourStepParams {
   uint32_t* jobs;                  // [n_out][maxjobs] job list per output spectrum
   uint32_t* njobs;                 // [n_out]
   uint32_t* dc;                    // [n_out][2] frames without data per gate
+  unsigned long long* dcsum;       // [n_out][maxjobs][6] exact DC sums of each job (see exact_dc)
   float* bsum;                     // pass B row-pair sums of the launch: [nk][N1/2][VALS][N2 + 1]
   // tensor-core form (form != 0): DFT-32 operand halves and W1024 twiddles
   uint32_t form;                   // GSPEC_FORM_*

@@ -264,18 +264,19 @@ __global__ void __launch_bounds__(PassALayout::THREADS, 2) tc_a_kernel(FourStepP
   static_assert((N1 + THREADS - 1) / THREADS * SP <= 128 && THREADS <= 512,
                 "per-thread gate statistics fit the 32-bit commit");
   GateStats st[NPOL];
+  DcAcc dc[2];
   for (int n1 = tid; n1 < N1; n1 += THREADS) {
     const uint32_t off = N2 * n1 + gbase;
     float re[SP], im[SP];
     if constexpr (DUAL) {
       gate_group_dual<NBITS, SP>(p.c.g, frA * N + off, bl[ga], bl[2 + ga], ga, re, im, st[0], st[NPOL - 1],
-                                 count_stats);
+                                 count_stats, &dc[0], &dc[1]);
     } else if (fb == fa) {
-      gate_group<NBITS, SP>(p.c.g, 0, frA * N + off, bl[0], bl[1], re, im, st[0], sg_a);
+      gate_group<NBITS, SP>(p.c.g, 0, frA * N + off, bl[0], bl[1], re, im, st[0], sg_a, &dc[0], &dc[1]);
     } else {
-      gate_group1<NBITS, SP>(p.c.g, 0, frA * N + off, bl[ga], ga, re, st[0], count_stats);
+      gate_group1<NBITS, SP>(p.c.g, 0, frA * N + off, bl[ga], ga, re, st[0], count_stats, &dc[0]);
       if (fb != kNoFrame) {
-        gate_group1<NBITS, SP>(p.c.g, 0, frB * N + off, bl[gb], gb, im, st[0], count_stats);
+        gate_group1<NBITS, SP>(p.c.g, 0, frB * N + off, bl[gb], gb, im, st[0], count_stats, &dc[1]);
       } else {
 #pragma unroll
         for (int e = 0; e < SP; ++e) im[e] = 0.f;
@@ -315,7 +316,8 @@ __global__ void __launch_bounds__(PassALayout::THREADS, 2) tc_a_kernel(FourStepP
       dst[static_cast<size_t>(k1) * N2 + n2] = cmul(Sc[spad(k1)], W);
     }
   }
-  commit_stats<NPOL>(p.c, st, k, (DUAL ? 8 : 2) * static_cast<int>(N / 2 + 1), red);
+  commit_stats<NPOL>(p.c, st, k, (DUAL ? 8 : 2) * static_cast<int>(N / 2 + 1), red, dc,
+                     p.dcsum + (static_cast<size_t>(k) * p.maxjobs + j) * 6);
   fence_after();
   if (tid < 32) tmem_dealloc(*tmem_slot, 2 * kTmemCols);
 }
@@ -442,8 +444,9 @@ __global__ void __launch_bounds__(kPassThreads, 2) tc_b_kernel(FourStepParams p)
       pair_slot<N2>(rp, a, r, k2, pr, k2p);
       for (int qq = 0; qq < nq; ++qq) {
         const uint32_t job = jw[qq];
-        const float2 za = work[(2 * qq + r) * kRowStride + spad(k2)];
-        const float2 zb = work[(2 * qq + pr) * kRowStride + spad(k2p)];
+        float2 za = work[(2 * qq + r) * kRowStride + spad(k2)];
+        float2 zb = work[(2 * qq + pr) * kRowStride + spad(k2p)];
+        if (rp == 0 && a == 0) za = zb = exact_dc(p, k, j0 + qq, job, DUAL);
         const uint32_t ga = job_ga(job);
         if constexpr (!DUAL) {
           const float sx = za.x + zb.x, sy = za.y - zb.y;

@@ -7,6 +7,12 @@
 //
 // Reads a 4096-byte header and then whole blocks, writes the 4096-byte header
 // (with the spectrometer parameters appended) and every output block.
+//
+// Built with -DUSE_REFERENCE_TYPES the program uses the reference's own type
+// names and signatures instead of the stand-alone ones: psrdada_cpp::RawBytes
+// and psrdada_cpp::effelsberg::edd::DadaBufferLayout constructed from a ring
+// key, as edd/src/GatedSpectrometer_cli.cu:45-102 does (header-only
+// stand-ins in reference_types_mock.hpp).
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -15,7 +21,12 @@
 
 #include "psrdada_cpp_gb300/GatedSpectrometer.hpp"
 
+#ifdef USE_REFERENCE_TYPES
+#include "reference_types_mock.hpp"
+using psrdada_cpp::RawBytes;
+#else
 using psrdada_cpp_gb300::RawBytes;
+#endif
 
 struct FileSink {
   std::ofstream out;
@@ -49,8 +60,15 @@ int main(int argc, char** argv) {
     return 2;
   }
   const std::size_t block = std::strtoull(argv[3], nullptr, 10);
+#ifdef USE_REFERENCE_TYPES
+  const key_t input_key = 0xdada;
+  psrdada_cpp::mock_rings()[input_key] = block;
+  psrdada_cpp::effelsberg::edd::DadaBufferLayout layout(input_key, std::strtoull(argv[4], nullptr, 10),
+                                                         std::strtoull(argv[5], nullptr, 10));
+#else
   psrdada_cpp_gb300::DadaBufferLayout layout(block, std::strtoull(argv[4], nullptr, 10),
                                               std::strtoull(argv[5], nullptr, 10));
+#endif
   const std::size_t fft = std::strtoull(argv[6], nullptr, 10), nacc = std::strtoull(argv[7], nullptr, 10);
   const std::size_t nbits = std::strtoull(argv[8], nullptr, 10);
   FileSink sink(argv[2]);
@@ -58,12 +76,12 @@ int main(int argc, char** argv) {
     std::size_t n;
     if (std::atoi(argv[9])) {
       psrdada_cpp_gb300::GatedSpectrometer<FileSink, psrdada_cpp_gb300::DualPolarizationInput,
-                                           psrdada_cpp_gb300::GatedFullStokesOutput>
+                                           psrdada_cpp_gb300::GatedFullStokesOutput, RawBytes>
           spec(layout, 0, 0, fft, nacc, nbits, 100.f, 100.f, sink);
       n = file_input_stream(argv[1], block, spec);
     } else {
       psrdada_cpp_gb300::GatedSpectrometer<FileSink, psrdada_cpp_gb300::SinglePolarizationInput,
-                                           psrdada_cpp_gb300::GatedPowerSpectrumOutput>
+                                           psrdada_cpp_gb300::GatedPowerSpectrumOutput, RawBytes>
           spec(layout, 0, 0, fft, nacc, nbits, 100.f, 100.f, sink);
       n = file_input_stream(argv[1], block, spec);
     }

@@ -17,13 +17,17 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
+@pytest.mark.parametrize("ref_types", [False, True], ids=["own_types", "reference_types"])
 @pytest.mark.parametrize("dual", [False, True])
-def test_cpp_file_pipeline(tmp_path, dual):
+def test_cpp_file_pipeline(tmp_path, dual, ref_types):
+    """ref_types: the same program built against the reference's RawBytes and
+    key-constructed DadaBufferLayout (header-only stand-ins)."""
     G.load_library()
     pkg = os.path.join(ROOT, "psrdada_cpp_gb300")
     exe = str(tmp_path / "pipeline")
-    r = subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
-                        os.path.join(ROOT, "tests", "cpp", "compile_handler.cpp"), "-o", exe,
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include")]
+                       + (["-DUSE_REFERENCE_TYPES"] if ref_types else []) +
+                       [os.path.join(ROOT, "tests", "cpp", "compile_handler.cpp"), "-o", exe,
                         "-L", pkg, "-lgspec", "-Wl,-rpath," + pkg], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     if dual:
