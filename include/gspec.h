@@ -175,6 +175,14 @@ int gspec_set_baselines(gspec_handle* h, const float* in4);
  * gspec_process (new in this library; no counterpart in the reference). */
 int gspec_get_saturation(gspec_handle* h, uint64_t* out);
 
+/* Page-locks (and maps) bytes of host memory at ptr for the current CUDA
+ * context, so that gspec_process copies blocks from it at the host link's
+ * full rate; replaces dada_cuda_dbregister, which DadaClientBase calls on
+ * attach to register a ring's blocks (psrdada_cpp/src/dada_client_base.cpp:78-88).
+ * gspec_unregister_host undoes it (before the memory is freed). */
+int gspec_register_host(void* ptr, size_t bytes);
+int gspec_unregister_host(void* ptr);
+
 /* Allocation-free variant of gspec_run_block_device (no counterpart in the
  * reference).  For callers that cannot allocate device memory between blocks
  * (device memory reserved up front by a ring buffer or an outside pool,

@@ -20,27 +20,9 @@
 #include <string>
 
 #include "../gspec.h"
+#include "raw_bytes.hpp"
 
 namespace psrdada_cpp_gb300 {
-
-// Non-owning view of a buffer, as psrdada_cpp::RawBytes.
-class RawBytes {
- public:
-  RawBytes(char* ptr, std::size_t total, std::size_t used = 0, bool device_memory = false)
-      : _ptr(ptr), _total(total), _used(used), _on_device(device_memory) {}
-  RawBytes(const RawBytes&) = delete;
-  std::size_t total_bytes() const { return _total; }
-  std::size_t used_bytes() const { return _used; }
-  void used_bytes(std::size_t u) { _used = u; }
-  char* ptr() { return _ptr; }
-  bool on_device() const { return _on_device; }
-
- private:
-  char* _ptr;
-  std::size_t _total;
-  std::size_t _used;
-  bool _on_device;
-};
 
 // DadaBufferLayout (psrdada_cpp/effelsberg/edd/DadaBufferLayout.hpp:20-54).
 // The reference reads the buffer size from the ring buffer

@@ -275,6 +275,9 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
     // job lists of every output spectrum of the block
     f.k0 = 0;
     f.nk = static_cast<uint32_t>(h->n_out);
+    // the exact DC sums of every job are accumulated by pass A
+    e = cudaMemsetAsync(h->d_dcsum, 0, 6ull * h->n_out * h->maxjobs * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
     e = timed(h, 7, s, [&] { return launch_fourstep(N, h->cfg.nbits, h->dual, f, -1, s); });
     if (e != cudaSuccess) return e;
     for (uint64_t k0 = 0; k0 < h->n_out; k0 += h->kchunk) {
@@ -792,6 +795,18 @@ int gspec_set_baselines(gspec_handle* h, const float* in4) {
       !cuda_ok(h, cudaMemcpy(h->d_baselines, in4, 4 * sizeof(float), cudaMemcpyHostToDevice), "baselines"))
     return GSPEC_ERR_CUDA;
   return GSPEC_OK;
+}
+
+int gspec_register_host(void* ptr, size_t bytes) {
+  if (!ptr || !bytes) return GSPEC_ERR_ARG;
+  return cudaHostRegister(ptr, bytes, cudaHostRegisterPortable | cudaHostRegisterMapped) == cudaSuccess
+             ? GSPEC_OK
+             : GSPEC_ERR_CUDA;
+}
+
+int gspec_unregister_host(void* ptr) {
+  if (!ptr) return GSPEC_ERR_ARG;
+  return cudaHostUnregister(ptr) == cudaSuccess ? GSPEC_OK : GSPEC_ERR_CUDA;
 }
 
 int gspec_get_saturation(gspec_handle* h, uint64_t* out) {

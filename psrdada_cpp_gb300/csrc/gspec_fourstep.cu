@@ -25,7 +25,6 @@ __global__ void fourstep_plan_kernel(FourStepParams p, int dual) {
   const uint32_t kk = blockIdx.x * blockDim.x + threadIdx.x;
   if (kk >= p.nk) return;
   const uint32_t k = p.k0 + kk;
-  for (uint32_t i = 0; i < 6 * p.maxjobs; ++i) p.dcsum[static_cast<size_t>(k) * p.maxjobs * 6 + i] = 0ull;
   uint32_t dc[2];
   p.njobs[k] = build_jobs(p.c.flags + k * p.c.nacc, p.c.nacc, dual != 0, p.jobs + k * p.maxjobs, dc);
   p.dc[2 * k] = dc[0];
@@ -305,41 +304,19 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, GSPEC_PASSB_MINB)
       pair_slot<N2>(rp, a, r, k2, pr, k2p);
       for (int qq = 0; qq < nq; ++qq) {
         const uint32_t job = jw[qq];
-        float2 za = work[(2 * qq + r) * Cfg::STRIDE + spad(k2)];
-        float2 zb = work[(2 * qq + pr) * Cfg::STRIDE + spad(k2p)];
-        if (rp == 0 && a == 0) za = zb = exact_dc(p, k, j0 + qq, job, DUAL);
-        const uint32_t ga = job_ga(job);
-        if constexpr (!DUAL) {
-          const float sx = za.x + zb.x, sy = za.y - zb.y;
-          const float dx = za.x - zb.x, dy = za.y + zb.y;
-          const float pa = 0.25f * fmaf(sx, sx, sy * sy);
-          const float pb = job_fb(job) != kNoFrame ? 0.25f * fmaf(dx, dx, dy * dy) : 0.f;
-          const uint32_t gb = job_gb(job);
-          acc[i][0] += (ga == 0 ? pa : 0.f) + (gb == 0 ? pb : 0.f);
-          acc[i][1] += (ga == 1 ? pa : 0.f) + (gb == 1 ? pb : 0.f);
-        } else {
-          const float p1x = 0.5f * (za.x + zb.x), p1y = 0.5f * (za.y - zb.y);
-          const float p2x = 0.5f * (za.y + zb.y), p2y = -0.5f * (za.x - zb.x);
-          const float a1 = fmaf(p1x, p1x, p1y * p1y);
-          const float a2 = fmaf(p2x, p2x, p2y * p2y);
-          const float I = a1 + a2, Q = a1 - a2;
-          const float U = 2.f * fmaf(p1x, p2x, p1y * p2y);
-          const float V = -2.f * fmaf(p1y, p2x, -p1x * p2y);
-          if (ga == 0) {
-            acc[i][0] += I;
-            acc[i][2] += Q;
-            acc[i][4] += U;
-            acc[i][6] += V;
-          } else {
-            acc[i][1] += I;
-            acc[i][3] += Q;
-            acc[i][5] += U;
-            acc[i][7] += V;
-          }
-        }
+        const float2 za = work[(2 * qq + r) * Cfg::STRIDE + spad(k2)];
+        const float2 zb = work[(2 * qq + pr) * Cfg::STRIDE + spad(k2p)];
+        accumulate_bin<DUAL>(acc[i], za, zb, job);
       }
     }
     __syncthreads();
+  }
+  // bin 0 from the exact per-job sums (exact_dc), over the jobs in order
+  if (rp == 0 && tid == 0) {
+    float d[VALS];
+    exact_dc_bin<DUAL>(p, k, d);
+#pragma unroll
+    for (int v = 0; v < VALS; ++v) acc[0][v] = d[v];
   }
   // gates without data: constant baseline in bin 0 (row pair 0, slot a = 0)
   if (rp == 0 && tid == 0) {

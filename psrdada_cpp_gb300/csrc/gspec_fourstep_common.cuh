@@ -97,6 +97,45 @@ __device__ __forceinline__ void pair_slot(uint32_t rp, int a, int& r, int& k2, i
   }
 }
 
+// Adds one job's contribution to the sums of one bin of a row pair: za is
+// Z[k] and zb Z[N-k] of the job's packed complex sequence z = a + i b.
+// Power: |A|^2 to a's gate and |B|^2 to b's gate
+// (edd/DetectorAccumulator.cuh:40-61); Stokes (dual pol, a = pol 0,
+// b = pol 1): I, Q, U, V (edd/src/GatedSpectrometer.cu:125-131) to the job's
+// gate.  acc holds [G0, G1] (power) or [I0, I1, Q0, Q1, U0, U1, V0, V1].
+template <bool DUAL, int VALS>
+__device__ __forceinline__ void accumulate_bin(float (&acc)[VALS], float2 za, float2 zb, uint32_t job) {
+  const uint32_t ga = job_ga(job);
+  if constexpr (!DUAL) {
+    const float sx = za.x + zb.x, sy = za.y - zb.y;
+    const float dx = za.x - zb.x, dy = za.y + zb.y;
+    const float pa = 0.25f * fmaf(sx, sx, sy * sy);
+    const float pb = job_fb(job) != kNoFrame ? 0.25f * fmaf(dx, dx, dy * dy) : 0.f;
+    const uint32_t gb = job_gb(job);
+    acc[0] += (ga == 0 ? pa : 0.f) + (gb == 0 ? pb : 0.f);
+    acc[1] += (ga == 1 ? pa : 0.f) + (gb == 1 ? pb : 0.f);
+  } else {
+    const float p1x = 0.5f * (za.x + zb.x), p1y = 0.5f * (za.y - zb.y);
+    const float p2x = 0.5f * (za.y + zb.y), p2y = -0.5f * (za.x - zb.x);
+    const float a1 = fmaf(p1x, p1x, p1y * p1y);
+    const float a2 = fmaf(p2x, p2x, p2y * p2y);
+    const float I = a1 + a2, Q = a1 - a2;
+    const float U = 2.f * fmaf(p1x, p2x, p1y * p2y);
+    const float V = -2.f * fmaf(p1y, p2x, -p1x * p2y);
+    if (ga == 0) {
+      acc[0] += I;
+      acc[2] += Q;
+      acc[4] += U;
+      acc[6] += V;
+    } else {
+      acc[1] += I;
+      acc[3] += Q;
+      acc[5] += U;
+      acc[7] += V;
+    }
+  }
+}
+
 // Bin 0 of job j of output spectrum k, computed exactly: the real and the
 // imaginary packed sequence each sum to (integer in-gate sum) + (residues) +
 // (N - in-gate count) * baseline, evaluated in FP64 and rounded once.  An FP32
@@ -117,6 +156,20 @@ __device__ __forceinline__ float2 exact_dc(const FourStepParams& p, uint32_t k, 
                         : static_cast<double>(d[3]) + static_cast<double>(d[5]) * 0x1p-24 +
                               (n - static_cast<double>(d[4])) * b_im;
   return make_float2(static_cast<float>(re), static_cast<float>(im));
+}
+
+// The sums of bin 0 (slot 0 of row pair 0) recomputed from the exact DC of
+// every job of output spectrum k, in job order (replacing the FFT's bin 0).
+template <bool DUAL, int VALS>
+__device__ __noinline__ void exact_dc_bin(const FourStepParams& p, uint32_t k, float (&acc)[VALS]) {
+#pragma unroll
+  for (int v = 0; v < VALS; ++v) acc[v] = 0.f;
+  const uint32_t nj = p.njobs[k];
+  for (uint32_t j = 0; j < nj; ++j) {
+    const uint32_t job = p.jobs[k * p.maxjobs + j];
+    const float2 z = exact_dc(p, k, j, job, DUAL);
+    accumulate_bin<DUAL>(acc, z, z, job);
+  }
 }
 
 }  // namespace gspec

@@ -107,6 +107,8 @@ def load_library() -> ctypes.CDLL:
     lib.gspec_process_block_noalloc.argtypes = [ctypes.POINTER(GspecConfig), vp, vp, vp, vp, ctypes.c_char_p, sz]
     lib.gspec_query.argtypes = [ctypes.POINTER(GspecConfig), ctypes.POINTER(GspecInfo), ctypes.c_char_p, sz]
     lib.gspec_tc_dft1024_device.argtypes = [vp, vp, u32, ctypes.c_int, vp]
+    lib.gspec_register_host.argtypes = [vp, sz]
+    lib.gspec_unregister_host.argtypes = [vp]
     from . import serving
     serving.declare(lib)
     _LIB = lib
