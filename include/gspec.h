@@ -50,6 +50,13 @@ extern "C" {
 #define GSPEC_FLAG_SATURATION_RECORD 1u /* append n_out x {sat G0, sat G1} u64 to each output */
 #define GSPEC_FLAG_NO_HOST_BUFFERS 2u   /* no pinned output buffers: the handle is driven only through
                                            gspec_run_block_device, a gspec_server or a gspec_batch */
+#define GSPEC_FLAG_UNGATED 4u         /* the ungated FFT spectrometer (FftSpectrometer,
+                                          edd/FftSpectrometer.cuh:19-85): the block holds only
+                                          samples (n_side_channels 0, heap_size ignored), every
+                                          sample is transformed as it is (no gate, no baseline),
+                                          single-pol power only; the handler receives n_out x
+                                          nchans float32 power spectra per output block and init()
+                                          appends nothing to the header */
 
 typedef struct gspec_config {
   /* DadaBufferLayout (edd/DadaBufferLayout.hpp:20-54): the reference reads the

@@ -511,6 +511,27 @@ def process_block_chunked(block: np.ndarray, cfg: Config, states: list, period_c
 
 
 # --------------------------------------------------------------------------
+# The ungated FftSpectrometer (edd/detail/FftSpectrometer.cu:13-179)
+# --------------------------------------------------------------------------
+def fft_spectrometer_block(block: np.ndarray, nbits: int, fft_length: int, naccumulate: int) -> np.ndarray:
+    """One block of ``FftSpectrometer::process``: unpack the whole block
+    (``edd/detail/FftSpectrometer.cu:93-99``), R2C every ``fft_length``
+    samples (``:101-107``) and sum ``|X|^2`` over groups of ``naccumulate``
+    frames (``detect_and_accumulate<float>``, ``edd/DetectorAccumulator.cuh:40-61``).
+    The intended frame count (all frames of the block) and a fresh sum per
+    block are used; the reference's in-place stride overlap, frame-count
+    rounding and never-cleared output buffers are defects.  Returns
+    [n_out, fft_length/2 + 1] power spectra in FP64."""
+    v = unpack(np.asarray(block, np.uint8), nbits)
+    n = v.size // fft_length
+    if n % naccumulate:
+        raise ValueError("frames per block not a multiple of naccumulate")
+    X = rfft64(v[:n * fft_length].astype(np.float32).reshape(n, fft_length))
+    C = fft_length // 2 + 1
+    return (np.abs(X) ** 2).reshape(n // naccumulate, naccumulate, C).sum(axis=1)
+
+
+# --------------------------------------------------------------------------
 # R13 / R14: output block layout
 # --------------------------------------------------------------------------
 def output_bytes(spectra: np.ndarray, n0: np.ndarray, n1: np.ndarray, dual_pol: bool) -> bytes:

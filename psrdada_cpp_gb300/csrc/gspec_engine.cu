@@ -52,11 +52,23 @@ int group_samples(int nbits) { return nbits == 8 ? 8 : (nbits == 10 ? 32 : 16); 
 
 // Validates the configuration and fills the derived sizes.
 bool configure(gspec_handle* h) {
-  const gspec_config& c = h->cfg;
   auto fail = [&](const std::string& m) {
     h->err = m;
     return false;
   };
+  // the ungated FFT spectrometer: the whole block is one "heap" of samples
+  // with one virtual side-channel item that puts every sample into gate 0
+  h->ungated = (h->cfg.flags & GSPEC_FLAG_UNGATED) != 0;
+  if (h->ungated) {
+    if (h->cfg.n_side_channels != 0) return fail("the ungated spectrometer's blocks hold samples only (n_side_channels 0)");
+    if (h->cfg.input_type != GSPEC_SINGLE_POL || h->cfg.output_type != GSPEC_POWER)
+      return fail("the ungated spectrometer takes single-pol samples and gives power spectra");
+    if (h->cfg.convention != GSPEC_INTENDED) return fail("the ungated spectrometer has no gate convention");
+    h->cfg.heap_size = h->cfg.buffer_size;
+    h->cfg.selected_side_channel = 0;
+    h->cfg.selected_bit = 0;
+  }
+  const gspec_config& c = h->cfg;
   if (c.nbits != 8 && c.nbits != 10 && c.nbits != 12) return fail("nbits must be 8, 10 or 12");
   if (c.input_type > 1 || c.output_type > 1) return fail("unknown input or output type");
   if (c.input_type == GSPEC_DUAL_POL && c.output_type == GSPEC_POWER)
@@ -66,8 +78,8 @@ bool configure(gspec_handle* h) {
   if (c.convention > 1) return fail("unknown gate convention");
   if (c.naccumulate == 0) return fail("naccumulate must be > 0");
   if (c.selected_bit >= 64) return fail("selected_bit must be < 64");
-  if (c.n_side_channels == 0) return fail("at least one side-channel item per heap is required");
-  if (c.selected_side_channel >= c.n_side_channels) return fail("selected_side_channel out of range");
+  if (c.n_side_channels == 0 && !h->ungated) return fail("at least one side-channel item per heap is required");
+  if (c.selected_side_channel >= c.n_side_channels && !h->ungated) return fail("selected_side_channel out of range");
   if (c.heap_size == 0) return fail("heap_size must be > 0");
   const uint64_t N = c.fft_length;
   if (N == 0 || (N & (N - 1))) return fail("fft_length must be a power of two");
@@ -116,6 +128,7 @@ bool configure(gspec_handle* h) {
   if (h->nsamps >= (1ull << 32)) return fail("more than 2^32 samples per pol");
   if (pol_bytes >= (1ull << 32)) return fail("more than 4 GiB of samples per pol in one block");
   h->items_per_pol = h->dual ? h->n_heaps * c.n_side_channels / 2 : h->n_heaps * c.n_side_channels;
+  if (h->ungated) h->items_per_pol = 1;
   const int gb = group_bytes(c.nbits);
   if (h->dual && (c.heap_size % gb)) {
     return fail("dual-pol heap size must be a multiple of " + std::to_string(gb) + " bytes");
@@ -147,6 +160,8 @@ bool configure(gspec_handle* h) {
   h->C = N / 2 + 1;
   h->rec = (h->dual ? 8 : 2) * (h->C * 4 + 8);
   h->out_bytes = h->rec * h->n_out;
+  // handed to the handler: the records, or the gate-0 spectra alone
+  h->hand_bytes = h->ungated ? h->n_out * h->C * 4 : h->out_bytes;
   h->ext_bytes = h->n_out * 16;
   if (c.convention == GSPEC_REFERENCE) {
     const uint64_t L = h->nsamps / h->n_out;
@@ -237,10 +252,16 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
   const int N = static_cast<int>(h->cfg.fft_length);
   cudaError_t e;
   // gate masks per item and the gates each frame holds data in
-  e = timed(h, 5, s, [&] {
-    return launch_prepass(p.g, static_cast<uint32_t>(h->items_per_pol), h->d_masks, static_cast<uint32_t>(N),
-                          static_cast<uint32_t>(h->batch), h->d_flags, s);
-  });
+  if (h->ungated) {
+    // one item, in gate 0; every frame holds gate-0 data only
+    e = cudaMemsetAsync(h->d_masks, 1, 1, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->d_flags, 1, h->batch, s);
+  } else {
+    e = timed(h, 5, s, [&] {
+      return launch_prepass(p.g, static_cast<uint32_t>(h->items_per_pol), h->d_masks, static_cast<uint32_t>(N),
+                            static_cast<uint32_t>(h->batch), h->d_flags, s);
+    });
+  }
   if (e != cudaSuccess) return e;
   if (h->path == 0) {
     e = timed(h, 0, s, [&] { return launch_small_chain(N, h->cfg.nbits, h->dual, p, s); });
@@ -252,6 +273,7 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
                                       s);
       });
       if (e != cudaSuccess) return e;
+      if (h->ungated && (e = cudaMemsetAsync(h->d_baselines, 0, 4 * sizeof(float), s)) != cudaSuccess) return e;
       return refresh_error_word(h, s);
     }
   } else {
@@ -297,6 +319,8 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
                            h->d_baselines, s);
   });
   if (e != cudaSuccess) return e;
+  // no gate, no baseline: the samples enter the FFT as they are ((v - 0) + 0 = v)
+  if (h->ungated && (e = cudaMemsetAsync(h->d_baselines, 0, 4 * sizeof(float), s)) != cudaSuccess) return e;
   return refresh_error_word(h, s);
 }
 
@@ -324,7 +348,7 @@ void release(gspec_handle* h) {
   }
   void* ptrs[] = {h->d_sat_dev, h->d_baselines, h->d_pol_stats, h->d_tw,   h->d_tw1,   h->d_tw2,  h->d_twA,
                   h->d_twB,     h->d_partial,   h->d_scratch,   h->d_masks, h->d_flags, h->d_jobs, h->d_njobs,
-                  h->d_dc,      h->d_err,       h->d_tc_hi,     h->d_tc_lo, h->d_tc_w, h->d_tc_img, h->d_bsum,
+                  h->d_dc,      h->d_err,       h->d_tc_parts,  h->d_tc_w,  h->d_tc_img, h->d_bsum,
                   h->d_dcsum};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -386,7 +410,16 @@ int do_process(gspec_handle* h, const void* block, size_t used, gspec_output* ou
   if (!(h->call_count == 2 || !new_block)) {
     const int ob = h->oa ^ 1;
     if (!cuda_ok(h, cudaStreamWaitEvent(h->d2h, h->ev_out_ready[ob], 0), "wait output")) return GSPEC_ERR_CUDA;
-    if (h->out_bytes + h->ext_bytes <= kStoreOutputMax) {
+    if (h->ungated) {
+      // the gate-0 spectrum of every record, packed (FftSpectrometer's output)
+      if (!cuda_ok(h, cudaMemcpy2DAsync(h->h_out[h->ha], h->C * 4, h->d_out[ob], h->rec, h->C * 4, h->n_out,
+                                        cudaMemcpyDeviceToHost, h->d2h),
+                   "D2H spectra") ||
+          !cuda_ok(h, cudaMemcpyAsync(h->h_out[h->ha] + h->hand_bytes, h->d_sat[ob], h->ext_bytes,
+                                      cudaMemcpyDeviceToHost, h->d2h),
+                   "D2H saturation"))
+        return GSPEC_ERR_CUDA;
+    } else if (h->out_bytes + h->ext_bytes <= kStoreOutputMax) {
       // SM stores into the pinned buffer: the host link then keeps its full
       // host-to-device rate for the next block's copy (a copy engine in each
       // direction at once takes ~170 GB/s from each)
@@ -411,7 +444,7 @@ int do_process(gspec_handle* h, const void* block, size_t used, gspec_output* ou
     if (h->call_count != 3 && h->host_written[h->ha ^ 1]) {
       h->handed = h->ha ^ 1;
       out->data = h->h_out[h->handed];
-      out->size = h->out_bytes + ((h->cfg.flags & GSPEC_FLAG_SATURATION_RECORD) ? h->ext_bytes : 0);
+      out->size = h->hand_bytes + ((h->cfg.flags & GSPEC_FLAG_SATURATION_RECORD) ? h->ext_bytes : 0);
       out->ready = 1;
     }
   }
@@ -509,7 +542,7 @@ uint64_t footprint(const gspec_handle* h) {
          sz(2ull * h->n_out * sizeof(uint32_t)) + sz(6ull * h->n_out * h->maxjobs * sizeof(unsigned long long));
     t += sz(bsum_bytes(h));
     if (h->cfg.form != GSPEC_FORM_FP32)
-      t += 2 * sz(4096 * sizeof(uint16_t)) + sz(1024 * sizeof(float2)) + sz(tc::kImageBytesHost);
+      t += sz(tc::kTableParts * 4096 * sizeof(uint16_t)) + sz(1024 * sizeof(float2)) + sz(tc::kImageBytesHost);
   }
   return t;
 }
@@ -520,7 +553,7 @@ void fill_info(const gspec_handle* h, gspec_info* info) {
   info->n_blocks = h->n_blocks;
   info->nsamps_per_pol = h->nsamps;
   info->batch = h->batch;
-  info->output_bytes = h->out_bytes + ((h->cfg.flags & GSPEC_FLAG_SATURATION_RECORD) ? h->ext_bytes : 0);
+  info->output_bytes = h->hand_bytes + ((h->cfg.flags & GSPEC_FLAG_SATURATION_RECORD) ? h->ext_bytes : 0);
   info->record_bytes = h->rec;
   info->device_bytes = h->device_bytes;
   info->fft_path = static_cast<uint64_t>(h->path);
@@ -633,14 +666,13 @@ gspec_handle* gspec_create(const gspec_config* cfg, char* err, size_t err_len) {
         !dalloc(h, &h->d_bsum, gspec_engine::bsum_bytes(h), "pass-B sums"))
       return bail("");
     if (cfg->form != GSPEC_FORM_FP32) {
-      if (!dalloc(h, &h->d_tc_hi, 4096 * sizeof(uint16_t), "tensor-core operand") ||
-          !dalloc(h, &h->d_tc_lo, 4096 * sizeof(uint16_t), "tensor-core operand") ||
+      if (!dalloc(h, &h->d_tc_parts, tc::kTableParts * 4096 * sizeof(uint16_t), "tensor-core operand") ||
           !dalloc(h, &h->d_tc_w, 1024 * sizeof(float2), "tensor-core twiddles") ||
           !dalloc(h, &h->d_tc_img, tc::kImageBytesHost, "tensor-core image"))
         return bail("");
-      if (!cuda_ok(h, tc::launch_tables(h->d_tc_hi, h->d_tc_lo, h->d_tc_w, cfg->form == GSPEC_FORM_BF16, h->proc),
+      if (!cuda_ok(h, tc::launch_tables(h->d_tc_parts, h->d_tc_w, cfg->form == GSPEC_FORM_BF16, h->proc),
                    "tensor-core tables") ||
-          !cuda_ok(h, tc::launch_image(h->d_tc_hi, h->d_tc_lo, h->d_tc_w, h->d_tc_img, h->proc), "tensor-core image"))
+          !cuda_ok(h, tc::launch_image(h->d_tc_parts, h->d_tc_w, h->d_tc_img, h->proc), "tensor-core image"))
         return bail("");
     }
   }
@@ -660,6 +692,8 @@ void gspec_destroy(gspec_handle* h) {
 
 int gspec_init(gspec_handle* h, char* header, size_t total_bytes) {
   if (!h || !header) return GSPEC_ERR_ARG;
+  // FftSpectrometer::init only forwards the header (edd/detail/FftSpectrometer.cu:119-123)
+  if (h->ungated) return GSPEC_OK;
   char text[512];
   const int n = std::snprintf(text, sizeof(text),
                               "\n# Gated spectrometer parameters: \n"
@@ -812,7 +846,7 @@ int gspec_unregister_host(void* ptr) {
 int gspec_get_saturation(gspec_handle* h, uint64_t* out) {
   if (!h || !out) return GSPEC_ERR_ARG;
   if (h->handed < 0) return set_err(h, GSPEC_ERR_STATE, "no output handed out yet");
-  std::memcpy(out, h->h_out[h->handed] + h->out_bytes, h->ext_bytes);
+  std::memcpy(out, h->h_out[h->handed] + h->hand_bytes, h->ext_bytes);
   return GSPEC_OK;
 }
 

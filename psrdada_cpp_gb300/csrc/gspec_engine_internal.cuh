@@ -19,9 +19,10 @@ struct gspec_handle {
   uint64_t n_heaps = 0, gap = 0, data_bytes = 0, sc_off = 0, sc_bytes = 0;
   // derived (edd/detail/GatedSpectrometer.cu:99-153)
   uint64_t nsamps = 0, items_per_pol = 0, n_blocks = 1, batch = 0, nacc = 0, n_out = 0, C = 0;
-  uint64_t rec = 0, out_bytes = 0, ext_bytes = 0;
+  uint64_t rec = 0, out_bytes = 0, ext_bytes = 0, hand_bytes = 0;
   int npol = 1;
   bool dual = false;
+  bool ungated = false;            // GSPEC_FLAG_UNGATED: the FftSpectrometer form
   int path = 0;
   uint32_t N1 = 0, N2 = 0;
   uint32_t slices = 1, frames_per_unit = 1;
@@ -50,10 +51,9 @@ struct gspec_handle {
   uint32_t* d_njobs = nullptr;
   uint32_t* d_dc = nullptr;
   unsigned long long* d_dcsum = nullptr;   // four-step: exact DC sums per job
-  uint16_t* d_tc_hi = nullptr;     // tensor-core form: DFT-32 operand halves
-  uint16_t* d_tc_lo = nullptr;
+  uint16_t* d_tc_parts = nullptr;  // tensor-core form: DFT-32 operand parts
   float2* d_tc_w = nullptr;        // W1024 twiddles
-  uint8_t* d_tc_img = nullptr;     // [B_hi | B_lo | W1024] in shared-memory layout
+  uint8_t* d_tc_img = nullptr;     // [B1 | B2 | B3 | W1024] in shared-memory layout
   float* d_bsum = nullptr;         // pass-B row-pair sums of one chunk
   uint32_t maxjobs = 0;
   int32_t heap_shift = -1;

@@ -14,25 +14,27 @@ namespace tc {
 // DFT-32 operand of one stage as a logical [n][k] 64 x 64 matrix with
 // n = 2c + s (output c, s = re/im) and k = 2a + r (input a, r = re/im):
 //   Yr = sum xr cos + xi sin,  Yi = sum -xr sin + xi cos,  angle 2 pi a c / 32,
-// split into hi + lo halves (BF16 or FP16 bit patterns) from FP64 values;
-// and the 1024 twiddles W1024^j = exp(-2 pi i j / 1024) in FP32 from FP64.
-__global__ void tables_kernel(uint16_t* hi, uint16_t* lo, float2* w1024, int bf16) {
+// split into kMaxParts parts (BF16 or FP16 bit patterns; part q is the
+// rounding of what parts 0..q-1 left of the FP64 value), stored as
+// parts[q * 4096 + 64 n + k]; and the 1024 twiddles W1024^j =
+// exp(-2 pi i j / 1024) in FP32 from FP64.
+__global__ void tables_kernel(uint16_t* parts, float2* w1024, int bf16) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 64 * 64; i += gridDim.x * blockDim.x) {
     const int n = i >> 6, k = i & 63;
     const int c = n >> 1, s = n & 1, a = k >> 1, r = k & 1;
     double sn, cs;
     sincospi(2.0 * ((a * c) & 31) / 32.0, &sn, &cs);
-    const double v = (s == 0) ? (r == 0 ? cs : sn) : (r == 0 ? -sn : cs);
-    if (bf16) {
-      const __nv_bfloat16 h = __double2bfloat16(v);
-      const __nv_bfloat16 l = __double2bfloat16(v - static_cast<double>(__bfloat162float(h)));
-      hi[i] = *reinterpret_cast<const uint16_t*>(&h);
-      lo[i] = *reinterpret_cast<const uint16_t*>(&l);
-    } else {
-      const __half h = __double2half(v);
-      const __half l = __double2half(v - static_cast<double>(__half2float(h)));
-      hi[i] = *reinterpret_cast<const uint16_t*>(&h);
-      lo[i] = *reinterpret_cast<const uint16_t*>(&l);
+    double v = (s == 0) ? (r == 0 ? cs : sn) : (r == 0 ? -sn : cs);
+    for (int q = 0; q < kMaxParts; ++q) {
+      if (bf16) {
+        const __nv_bfloat16 h = __double2bfloat16(v);
+        parts[q * 4096 + i] = *reinterpret_cast<const uint16_t*>(&h);
+        v -= static_cast<double>(__bfloat162float(h));
+      } else {
+        const __half h = __double2half(v);
+        parts[q * 4096 + i] = *reinterpret_cast<const uint16_t*>(&h);
+        v -= static_cast<double>(__half2float(h));
+      }
     }
   }
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < 1024; j += gridDim.x * blockDim.x) {
@@ -42,51 +44,50 @@ __global__ void tables_kernel(uint16_t* hi, uint16_t* lo, float2* w1024, int bf1
   }
 }
 
-cudaError_t launch_tables(uint16_t* hi, uint16_t* lo, float2* w1024, bool bf16, cudaStream_t s) {
-  tables_kernel<<<16, 256, 0, s>>>(hi, lo, w1024, bf16 ? 1 : 0);
+cudaError_t launch_tables(uint16_t* parts, float2* w1024, bool bf16, cudaStream_t s) {
+  tables_kernel<<<16, 256, 0, s>>>(parts, w1024, bf16 ? 1 : 0);
   return cudaGetLastError();
 }
 
-// The shared-memory image of [B_hi | B_lo | W1024] (canonical layout, pad
+// The shared-memory image of [B1 | B2 | B3 | W1024] (canonical layout, pad
 // bytes zero) that every tensor-core CTA copies with 16-byte loads.
-__global__ void image_kernel(const uint16_t* hi, const uint16_t* lo, const float2* w, uint8_t* img) {
+__global__ void image_kernel(const uint16_t* parts, const float2* w, uint8_t* img) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < static_cast<int>(kImageBytes); i += gridDim.x * blockDim.x)
     img[i] = 0;
   __syncthreads();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 64 * 64; i += gridDim.x * blockDim.x) {
     const int n = i >> 6, k = i & 63;
-    *reinterpret_cast<uint16_t*>(img + kmaj_off(n, k)) = hi[i];
-    *reinterpret_cast<uint16_t*>(img + kBBytes + kmaj_off(n, k)) = lo[i];
+    for (int q = 0; q < kMaxParts; ++q)
+      *reinterpret_cast<uint16_t*>(img + q * kBBytes + kmaj_off(n, k)) = parts[q * 4096 + i];
   }
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < 1024; j += gridDim.x * blockDim.x)
-    reinterpret_cast<float2*>(img + 2 * kBBytes)[j] = w[j];
+    reinterpret_cast<float2*>(img + kMaxParts * kBBytes)[j] = w[j];
 }
 
-cudaError_t launch_image(const uint16_t* hi, const uint16_t* lo, const float2* w, uint8_t* img, cudaStream_t s) {
-  image_kernel<<<1, 256, 0, s>>>(hi, lo, w, img);
+cudaError_t launch_image(const uint16_t* parts, const float2* w, uint8_t* img, cudaStream_t s) {
+  image_kernel<<<1, 256, 0, s>>>(parts, w, img);
   return cudaGetLastError();
 }
 
 // Test kernel: ntiles x 4 transforms of 1024 points, global in/out.
 template <bool BF16>
 __global__ void __launch_bounds__(128) dft1024_test_kernel(const float2* __restrict__ in, float2* __restrict__ out,
-                                                           const uint16_t* __restrict__ g_hi,
-                                                           const uint16_t* __restrict__ g_lo,
+                                                           const uint16_t* __restrict__ g_parts,
                                                            const float2* __restrict__ g_w, uint32_t* err) {
   extern __shared__ __align__(1024) char smem[];
   TileSmem s;
-  s.a_hi = smem;
-  s.a_lo = smem + kABytes;
-  s.b_hi = smem + 2 * kABytes;
-  s.b_lo = smem + 2 * kABytes + kBBytes;
-  float2* w = reinterpret_cast<float2*>(smem + 2 * kABytes + 2 * kBBytes);
+  for (int q = 0; q < kMaxParts; ++q) {
+    s.a[q] = smem + q * kABytes;
+    s.b[q] = smem + kMaxParts * kABytes + q * kBBytes;
+  }
+  float2* w = reinterpret_cast<float2*>(smem + kMaxParts * (kABytes + kBBytes));
   float2* xs = w + 1024;                                         // 4 x 1024 inputs, then outputs
   uint64_t* bar = reinterpret_cast<uint64_t*>(xs + 4 * 1024);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
   s.w = w;
   s.bar = bar;
   const int tid = threadIdx.x;
-  load_dft32_operand(s.b_hi, s.b_lo, g_hi, g_lo, tid, 128);
+  load_dft32_operand(s.b, g_parts, tid, 128);
   for (int i = tid; i < 1024; i += 128) w[i] = g_w[i];
   const float2* src = in + static_cast<size_t>(blockIdx.x) * 4 * 1024;
   for (int i = tid; i < 4 * 1024; i += 128) xs[i] = src[i];
@@ -111,7 +112,7 @@ __global__ void __launch_bounds__(128) dft1024_test_kernel(const float2* __restr
   if (tid < 32) tmem_dealloc(s.tmem, kCols);
 }
 
-size_t test_smem_bytes() { return 2 * kABytes + 2 * kBBytes + 1024 * 8 + 4 * 1024 * 8 + 16; }
+size_t test_smem_bytes() { return kMaxParts * (kABytes + kBBytes) + 1024 * 8 + 4 * 1024 * 8 + 16; }
 
 }  // namespace tc
 }  // namespace gspec
@@ -124,20 +125,20 @@ extern "C" int gspec_tc_dft1024_device(const void* d_in, void* d_out, uint32_t n
   if (form != GSPEC_FORM_BF16 && form != GSPEC_FORM_FP16) return GSPEC_ERR_ARG;
   const bool bf16 = form == GSPEC_FORM_BF16;
   cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
-  uint16_t *hi = nullptr, *lo = nullptr;
+  uint16_t* parts = nullptr;
   float2* w = nullptr;
   uint32_t* err = nullptr;
   int rc = GSPEC_OK;
-  if (cudaMalloc(&hi, 4096 * 2) != cudaSuccess || cudaMalloc(&lo, 4096 * 2) != cudaSuccess ||
+  if (cudaMalloc(&parts, tc::kMaxParts * 4096 * 2) != cudaSuccess ||
       cudaMalloc(&w, 1024 * sizeof(float2)) != cudaSuccess || cudaMalloc(&err, 4) != cudaSuccess) {
     rc = GSPEC_ERR_CUDA;
   } else {
     cudaMemsetAsync(err, 0, 4, s);
-    tc::launch_tables(hi, lo, w, bf16, s);
+    tc::launch_tables(parts, w, bf16, s);
     const size_t smem = tc::test_smem_bytes();
     auto kern = bf16 ? tc::dft1024_test_kernel<true> : tc::dft1024_test_kernel<false>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    kern<<<ntransforms / 4, 128, smem, s>>>(static_cast<const float2*>(d_in), static_cast<float2*>(d_out), hi, lo, w,
+    kern<<<ntransforms / 4, 128, smem, s>>>(static_cast<const float2*>(d_in), static_cast<float2*>(d_out), parts, w,
                                              err);
     uint32_t h_err = 0;
     if (cudaGetLastError() != cudaSuccess || cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -146,8 +147,7 @@ extern "C" int gspec_tc_dft1024_device(const void* d_in, void* d_out, uint32_t n
     else if (h_err)
       rc = GSPEC_ERR_CUDA;
   }
-  cudaFree(hi);
-  cudaFree(lo);
+  cudaFree(parts);
   cudaFree(w);
   cudaFree(err);
   return rc;
@@ -181,12 +181,13 @@ __device__ __forceinline__ void load_image(char* dst, const uint4* __restrict__ 
   for (int i = tid; i < static_cast<int>(kImageBytes / 16); i += nthreads) d[i] = __ldg(img + i);
 }
 
+template <bool BF16>
 struct PassALayout {
   static constexpr int BC = 8;                          // columns per CTA: two tiles of 4
   static constexpr int THREADS = 2 * kPassThreads;      // one 128-thread group per tile
-  static constexpr size_t A = 0;                        // per tile: operands, then its transformed columns
-  static constexpr size_t TILE = 2 * kABytes;
-  static constexpr size_t B = 2 * TILE;                 // [B_hi | B_lo | W1024]: the image
+  static constexpr size_t A = 0;                        // per tile: operand parts, then its transformed columns
+  static constexpr size_t TILE = Parts<BF16>::n * kABytes;
+  static constexpr size_t B = 2 * TILE;                 // [B1 | B2 | B3 | W1024]: the image
   static constexpr size_t RED = B + kImageBytes;
   static constexpr size_t BAR = RED + (THREADS / 32) * 12 * 8;
   static constexpr size_t BYTES = BAR + 32;
@@ -200,9 +201,9 @@ struct PassALayout {
 // transformed columns (written over the operands) leave with the
 // W_N^(n2*k1) twiddle.
 template <int NBITS, bool DUAL, bool BF16>
-__global__ void __launch_bounds__(PassALayout::THREADS, 2) tc_a_kernel(FourStepParams p) {
+__global__ void __launch_bounds__(PassALayout<BF16>::THREADS, Parts<BF16>::n == 3 ? 1 : 2) tc_a_kernel(FourStepParams p) {
   constexpr int N1 = 1024;
-  using L = PassALayout;
+  using L = PassALayout<BF16>;
   constexpr int BC = L::BC, THREADS = L::THREADS;
   constexpr int G = Group<NBITS>::samples;
   constexpr int NPOL = DUAL ? 2 : 1;
@@ -214,11 +215,11 @@ __global__ void __launch_bounds__(PassALayout::THREADS, 2) tc_a_kernel(FourStepP
   unsigned long long* red = reinterpret_cast<unsigned long long*>(smem + L::RED);
   auto tile_smem = [&](int g) {
     TileSmem t;
-    t.a_hi = smem + L::A + g * L::TILE;
-    t.a_lo = t.a_hi + kABytes;
-    t.b_hi = smem + L::B;
-    t.b_lo = smem + L::B + kBBytes;
-    t.w = reinterpret_cast<const float2*>(smem + L::B + 2 * kBBytes);
+    for (int q = 0; q < kMaxParts; ++q) {
+      t.a[q] = smem + L::A + g * L::TILE + (q < Parts<BF16>::n ? q : 0) * kABytes;
+      t.b[q] = smem + L::B + q * kBBytes;
+    }
+    t.w = reinterpret_cast<const float2*>(smem + L::B + kMaxParts * kBBytes);
     t.bar = bar + g;
     return t;
   };
@@ -293,7 +294,7 @@ __global__ void __launch_bounds__(PassALayout::THREADS, 2) tc_a_kernel(FourStepP
   fence_after();
   s.tmem = *tmem_slot + grp * kTmemCols;
   uint32_t phase = 0;
-  float2* S = reinterpret_cast<float2*>(s.a_hi);          // this tile's columns after the transform
+  float2* S = reinterpret_cast<float2*>(s.a[0]);          // this tile's columns after the transform
   const bool ok = dft1024_stages<BF16>(
       s, phase, gtid, [&](int t, int k1, float2 v) { S[t * kColStride + spad(k1)] = v; }, [] {}, sc1, sc2);
   if (!ok && gtid == 0 && p.c.dev_err) atomicExch(p.c.dev_err, 3u);
@@ -322,19 +323,20 @@ __global__ void __launch_bounds__(PassALayout::THREADS, 2) tc_a_kernel(FourStepP
   if (tid < 32) tmem_dealloc(*tmem_slot, 2 * kTmemCols);
 }
 
-template <bool DUAL>
+template <bool DUAL, bool BF16>
 struct PassBLayout {
   static constexpr int J = 2;                        // jobs per group: 2 jobs x 2 rows = one tile
   static constexpr int VALS = DUAL ? 8 : 2;
   static constexpr int BPT = (1024 + 1 + kPassThreads - 1) / kPassThreads;
-  static constexpr size_t A = 0;                     // operands; the transformed rows ("work") alias them
-  static constexpr size_t B = 2 * kABytes;            // [B_hi | B_lo | W1024]: the image
-  static constexpr size_t W = B + 2 * kBBytes;
+  static constexpr size_t A = 0;                     // operand parts; the transformed rows ("work") alias them
+  static constexpr size_t B = Parts<BF16>::n * kABytes;   // [B1 | B2 | B3 | W1024]: the image
+  static constexpr size_t W = B + kMaxParts * kBBytes;
   static constexpr size_t STAGE = W + 1024 * sizeof(float2);
   static constexpr size_t JW = STAGE + static_cast<size_t>(J) * 2 * 1024 * sizeof(float2);
   static constexpr size_t BAR = JW + 16;
   static constexpr size_t BYTES = BAR + 32;
-  static_assert(static_cast<size_t>(4) * kRowStride * sizeof(float2) <= 2 * kABytes, "work fits the operands");
+  static_assert(static_cast<size_t>(4) * kRowStride * sizeof(float2) <= Parts<BF16>::n * kABytes,
+                "work fits the operands");
 };
 
 // grid.x = nk * N1/2: unit (output spectrum k, row pair rp); jobs two at a
@@ -343,15 +345,15 @@ struct PassBLayout {
 template <bool DUAL, bool BF16>
 __global__ void __launch_bounds__(kPassThreads, 2) tc_b_kernel(FourStepParams p) {
   constexpr int N2 = 1024;
-  using L = PassBLayout<DUAL>;
+  using L = PassBLayout<DUAL, BF16>;
   constexpr int J = L::J, BPT = L::BPT, VALS = L::VALS;
   constexpr uint32_t kRowBytes = N2 * sizeof(float2);
   extern __shared__ __align__(1024) char smem[];
   TileSmem s;
-  s.a_hi = smem + L::A;
-  s.a_lo = smem + L::A + kABytes;
-  s.b_hi = smem + L::B;
-  s.b_lo = smem + L::B + kBBytes;
+  for (int q = 0; q < kMaxParts; ++q) {
+    s.a[q] = smem + L::A + (q < Parts<BF16>::n ? q : 0) * kABytes;
+    s.b[q] = smem + L::B + q * kBBytes;
+  }
   float2* work = reinterpret_cast<float2*>(smem + L::A);
   float2* stage = reinterpret_cast<float2*>(smem + L::STAGE);
   float2* w = reinterpret_cast<float2*>(smem + L::W);
@@ -503,22 +505,23 @@ template <bool BF16>
 static cudaError_t launch_pass(int pass, int nbits, bool dual, const FourStepParams& p, cudaStream_t s) {
   if (pass == 0) {
     if (p.N1 != 1024) return cudaErrorInvalidValue;
-    const unsigned grid = p.nk * p.maxjobs * (p.N2 / PassALayout::BC);
-    const size_t sm = PassALayout::BYTES;
+    using LA = PassALayout<BF16>;
+    const unsigned grid = p.nk * p.maxjobs * (p.N2 / LA::BC);
+    const size_t sm = LA::BYTES;
     switch (nbits * 2 + (dual ? 1 : 0)) {
-      case 16: return run_tc(tc_a_kernel<8, false, BF16>, grid, sm, p, s, PassALayout::THREADS);
-      case 17: return run_tc(tc_a_kernel<8, true, BF16>, grid, sm, p, s, PassALayout::THREADS);
-      case 20: return run_tc(tc_a_kernel<10, false, BF16>, grid, sm, p, s, PassALayout::THREADS);
-      case 21: return run_tc(tc_a_kernel<10, true, BF16>, grid, sm, p, s, PassALayout::THREADS);
-      case 24: return run_tc(tc_a_kernel<12, false, BF16>, grid, sm, p, s, PassALayout::THREADS);
-      case 25: return run_tc(tc_a_kernel<12, true, BF16>, grid, sm, p, s, PassALayout::THREADS);
+      case 16: return run_tc(tc_a_kernel<8, false, BF16>, grid, sm, p, s, LA::THREADS);
+      case 17: return run_tc(tc_a_kernel<8, true, BF16>, grid, sm, p, s, LA::THREADS);
+      case 20: return run_tc(tc_a_kernel<10, false, BF16>, grid, sm, p, s, LA::THREADS);
+      case 21: return run_tc(tc_a_kernel<10, true, BF16>, grid, sm, p, s, LA::THREADS);
+      case 24: return run_tc(tc_a_kernel<12, false, BF16>, grid, sm, p, s, LA::THREADS);
+      case 25: return run_tc(tc_a_kernel<12, true, BF16>, grid, sm, p, s, LA::THREADS);
     }
     return cudaErrorInvalidValue;
   }
   if (p.N2 != 1024) return cudaErrorInvalidValue;
   const unsigned grid = p.nk * (p.N1 / 2);
-  return dual ? run_tc(tc_b_kernel<true, BF16>, grid, PassBLayout<true>::BYTES, p, s)
-              : run_tc(tc_b_kernel<false, BF16>, grid, PassBLayout<false>::BYTES, p, s);
+  return dual ? run_tc(tc_b_kernel<true, BF16>, grid, PassBLayout<true, BF16>::BYTES, p, s)
+              : run_tc(tc_b_kernel<false, BF16>, grid, PassBLayout<false, BF16>::BYTES, p, s);
 }
 
 cudaError_t launch_tc_pass(int pass, int nbits, bool dual, const FourStepParams& p, cudaStream_t s) {

@@ -7,11 +7,24 @@
 // are the length-32 sub-sequences of four transforms (4 x 32 = 128 rows, the
 // M of one tcgen05.mma), K = 64 real inputs (re, im interleaved), N = 64 real
 // outputs (re, im interleaved), with the constant DFT-32 matrix as B.
-// Precision: operands are split into hi + lo halves in BF16 (or FP16) and
-// the product is accumulated in FP32 in tensor memory as
-//   A_hi B_hi + A_lo B_hi + A_hi B_lo,
-// 12 MMAs of K = 16 per stage; the dropped A_lo B_lo term is ~2^-16 of the
-// result in BF16.
+// Precision: operands are split into parts of the 16-bit type, each part the
+// rounding of what the parts before it left (x = x1 + x2 (+ x3) + r), and the
+// product is accumulated in FP32 in tensor memory from the partial products
+// whose parts together carry the leading bits:
+//   FP16 (11-bit parts, two per operand): A1 B1 + A1 B2 + A2 B1, 12 MMAs of
+//     K = 16 per stage; what is left is ~2^-22 of the result;
+//   BF16 (8-bit parts), GSPEC_BF16_PRODUCTS = 6: three parts per operand and
+//     the bf16x6 scheme of Henry, Tang and Heinecke ("Leveraging the bfloat16
+//     artificial intelligence datatype for higher-precision computations",
+//     ARITH 2019): A1 B1 + A1 B2 + A2 B1 + A2 B2 + A1 B3 + A3 B1, 24 MMAs per
+//     stage, ~2^-24 left over;
+//   BF16, GSPEC_BF16_PRODUCTS = 5: the data operand A in two parts, the
+//     constant DFT-32 matrix B in three, A1 B1 + A1 B2 + A2 B1 + A2 B2 +
+//     A1 B3 (20 MMAs): of the three 2^-18 terms of the two-part split (A's
+//     remainder, B's remainder, A2 B2) only A's remainder is left, and the
+//     operand build and shared memory are those of the two-part split.
+// The small products are issued first so that they are summed before the
+// large one joins the accumulator.
 //
 // Shared-memory operands use the canonical K-major layout without swizzle:
 // 8-row x 16-byte core matrices; element (row, k) of a bf16 matrix sits at
@@ -34,8 +47,21 @@ constexpr uint32_t kSBO = 8 * kLBO;              // 8 K-chunks of 8 elements per
 constexpr uint32_t kABytes = 16 * kSBO;          // 128 rows x 64 bf16
 constexpr uint32_t kBBytes = 8 * kSBO;           // 64 rows x 64 bf16
 constexpr uint32_t kTmemCols = 64;               // 128 lanes x 64 fp32 accumulators
-constexpr uint32_t kImageBytes = 2 * kBBytes + 1024 * 8;   // [B_hi | B_lo | W1024] in shared-memory layout
-static_assert(kImageBytes == 2 * 9216 + 1024 * 8, "image size as declared for the host");
+constexpr int kMaxParts = 3;
+constexpr uint32_t kImageBytes = kMaxParts * kBBytes + 1024 * 8;   // [B1 | B2 | B3 | W1024] in shared-memory layout
+static_assert(kImageBytes == 3 * 9216 + 1024 * 8, "image size as declared for the host");
+
+#ifndef GSPEC_BF16_PRODUCTS
+#define GSPEC_BF16_PRODUCTS 5
+#endif
+static_assert(GSPEC_BF16_PRODUCTS == 5 || GSPEC_BF16_PRODUCTS == 6, "BF16 split: 5 or 6 partial products");
+
+// parts of the data operand A (n) and partial products of a stage (products)
+template <bool BF16>
+struct Parts {
+  static constexpr int n = BF16 ? (GSPEC_BF16_PRODUCTS == 6 ? 3 : 2) : 2;
+  static constexpr int products = BF16 ? GSPEC_BF16_PRODUCTS : 3;
+};
 constexpr uint32_t kWaitLimit = 1u << 22;
 
 __host__ __device__ constexpr uint32_t kmaj_off(uint32_t row, uint32_t k) {
@@ -97,48 +123,67 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// hi/lo split of a complex value into two packed 16-bit pairs (re in the low half).
+// Split of a complex value into Parts<BF16>::n packed 16-bit pairs (re in
+// the low half): part i is the rounding of what parts 0..i-1 left; every
+// remainder is exact in FP32.
 template <bool BF16>
-__device__ __forceinline__ void split2(float2 v, uint32_t& hi, uint32_t& lo) {
-  if constexpr (BF16) {
-    const __nv_bfloat162 h = __floats2bfloat162_rn(v.x, v.y);
-    const float2 hf = __bfloat1622float2(h);
-    const __nv_bfloat162 l = __floats2bfloat162_rn(v.x - hf.x, v.y - hf.y);
-    hi = *reinterpret_cast<const uint32_t*>(&h);
-    lo = *reinterpret_cast<const uint32_t*>(&l);
-  } else {
-    const __half2 h = __floats2half2_rn(v.x, v.y);
-    const float2 hf = __half22float2(h);
-    const __half2 l = __floats2half2_rn(v.x - hf.x, v.y - hf.y);
-    hi = *reinterpret_cast<const uint32_t*>(&h);
-    lo = *reinterpret_cast<const uint32_t*>(&l);
+__device__ __forceinline__ void splitn(float2 v, uint32_t (&p)[Parts<BF16>::n]) {
+#pragma unroll
+  for (int i = 0; i < Parts<BF16>::n; ++i) {
+    if constexpr (BF16) {
+      const __nv_bfloat162 h = __floats2bfloat162_rn(v.x, v.y);
+      const float2 hf = __bfloat1622float2(h);
+      p[i] = *reinterpret_cast<const uint32_t*>(&h);
+      v = make_float2(v.x - hf.x, v.y - hf.y);
+    } else {
+      const __half2 h = __floats2half2_rn(v.x, v.y);
+      const float2 hf = __half22float2(h);
+      p[i] = *reinterpret_cast<const uint32_t*>(&h);
+      v = make_float2(v.x - hf.x, v.y - hf.y);
+    }
   }
 }
 
 // Shared memory of one tile engine (offsets from a 1024-byte aligned base).
 struct TileSmem {
-  char* a_hi;        // kABytes
-  char* a_lo;        // kABytes
-  char* b_hi;        // kBBytes (DFT-32 matrix)
-  char* b_lo;        // kBBytes
-  const float2* w;   // 1024 twiddles W1024^j
-  uint64_t* bar;     // MMA completion barrier
-  uint32_t tmem;     // TMEM base (kTmemCols columns)
+  char* a[kMaxParts];   // operand parts, kABytes each (the form uses Parts<BF16>::n)
+  char* b[kMaxParts];   // DFT-32 matrix parts, kBBytes each
+  const float2* w;      // 1024 twiddles W1024^j
+  uint64_t* bar;        // MMA completion barrier
+  uint32_t tmem;        // TMEM base (kTmemCols columns)
 };
 
-// Issues one stage: 12 MMAs (hi*hi, lo*hi, hi*lo over K = 64) and a commit.
+// (A part, B part) of the partial products of a stage, smallest first:
+// BF16 x6 (2,0) (0,2) (1,1) (1,0) (0,1) (0,0); BF16 x5 (1,1) (0,2) (1,0)
+// (0,1) (0,0); FP16 (1,0) (0,1) (0,0).
+template <bool BF16>
+__host__ __device__ constexpr int prod_a(int q) {
+  return !BF16 ? (q == 0 ? 1 : 0)
+               : Parts<true>::products == 6 ? (q == 0 ? 2 : q == 2 ? 1 : q == 3 ? 1 : 0)
+                                             : (q == 0 ? 1 : q == 2 ? 1 : 0);
+}
+template <bool BF16>
+__host__ __device__ constexpr int prod_b(int q) {
+  return !BF16 ? (q == 1 ? 1 : 0)
+               : Parts<true>::products == 6 ? (q == 1 ? 2 : q == 2 ? 1 : q == 4 ? 1 : 0)
+                                             : (q == 0 ? 1 : q == 1 ? 2 : q == 3 ? 1 : 0);
+}
+
+// Issues one stage (the form's partial products over K = 64, 4 MMAs of
+// K = 16 each, the smallest products first) and a commit.
 template <bool BF16>
 __device__ __forceinline__ void issue_stage(const TileSmem& s) {
   constexpr uint32_t id = idesc(128, 64, BF16);
-  const uint32_t ah = smem_addr(s.a_hi), al = smem_addr(s.a_lo);
-  const uint32_t bh = smem_addr(s.b_hi), bl = smem_addr(s.b_lo);
+  constexpr int NPROD = Parts<BF16>::products;
   fence_after();
 #pragma unroll
-  for (uint32_t ks = 0; ks < 4; ++ks) {
-    const uint32_t off = ks * 2 * kLBO;
-    mma(s.tmem, sdesc(ah + off), sdesc(bh + off), id, ks > 0 ? 1u : 0u);
-    mma(s.tmem, sdesc(al + off), sdesc(bh + off), id, 1u);
-    mma(s.tmem, sdesc(ah + off), sdesc(bl + off), id, 1u);
+  for (int q = 0; q < NPROD; ++q) {
+    const uint32_t a = smem_addr(s.a[prod_a<BF16>(q)]), b = smem_addr(s.b[prod_b<BF16>(q)]);
+#pragma unroll
+    for (uint32_t ks = 0; ks < 4; ++ks) {
+      const uint32_t off = ks * 2 * kLBO;
+      mma(s.tmem, sdesc(a + off), sdesc(b + off), id, (q > 0 || ks > 0) ? 1u : 0u);
+    }
   }
   commit(s.bar);
 }
@@ -149,11 +194,11 @@ __device__ __forceinline__ float2 scale2(float2 v, float f) { return make_float2
 // stored by whoever produces the value (scaled by sc1, split hi/lo).
 template <bool BF16>
 __device__ __forceinline__ void put_stage1(const TileSmem& s, int t, int n, float2 v, float sc1) {
-  uint32_t hi, lo;
-  split2<BF16>(scale2(v, sc1), hi, lo);
+  uint32_t p[Parts<BF16>::n];
+  splitn<BF16>(scale2(v, sc1), p);
   const uint32_t off = kmaj_off(32 * t + (n & 31), 2 * (n >> 5));
-  *reinterpret_cast<uint32_t*>(s.a_hi + off) = hi;
-  *reinterpret_cast<uint32_t*>(s.a_lo + off) = lo;
+#pragma unroll
+  for (int i = 0; i < Parts<BF16>::n; ++i) *reinterpret_cast<uint32_t*>(s.a[i] + off) = p[i];
 }
 
 // The two tensor-core stages of a tile whose stage-1 operands are in place
@@ -177,19 +222,21 @@ __device__ __forceinline__ bool dft1024_stages(const TileSmem& s, uint32_t& phas
 #pragma unroll
     for (int c = 0; c < 16; ++c) {
       const float2 z = scale2(cmul(make_float2(v[2 * c], v[2 * c + 1]), s.w[lane * c]), sc2);
-      uint32_t hi, lo;
-      split2<BF16>(z, hi, lo);
-      *reinterpret_cast<uint32_t*>(s.a_hi + kmaj_off(32 * t + c, 2 * lane)) = hi;
-      *reinterpret_cast<uint32_t*>(s.a_lo + kmaj_off(32 * t + c, 2 * lane)) = lo;
+      uint32_t p[Parts<BF16>::n];
+      splitn<BF16>(z, p);
+#pragma unroll
+      for (int i = 0; i < Parts<BF16>::n; ++i)
+        *reinterpret_cast<uint32_t*>(s.a[i] + kmaj_off(32 * t + c, 2 * lane)) = p[i];
     }
     tmem_ld32(lane_addr + 32, v);
 #pragma unroll
     for (int c = 0; c < 16; ++c) {
       const float2 z = scale2(cmul(make_float2(v[2 * c], v[2 * c + 1]), s.w[lane * (c + 16)]), sc2);
-      uint32_t hi, lo;
-      split2<BF16>(z, hi, lo);
-      *reinterpret_cast<uint32_t*>(s.a_hi + kmaj_off(32 * t + c + 16, 2 * lane)) = hi;
-      *reinterpret_cast<uint32_t*>(s.a_lo + kmaj_off(32 * t + c + 16, 2 * lane)) = lo;
+      uint32_t p[Parts<BF16>::n];
+      splitn<BF16>(z, p);
+#pragma unroll
+      for (int i = 0; i < Parts<BF16>::n; ++i)
+        *reinterpret_cast<uint32_t*>(s.a[i] + kmaj_off(32 * t + c + 16, 2 * lane)) = p[i];
     }
   }
   fence_before();
@@ -224,25 +271,27 @@ __device__ __forceinline__ bool dft1024_tile(const TileSmem& s, uint32_t& phase,
                                              float sc1 = 1.f, float sc2 = 1.f) {
   const int t = tid >> 5, lane = tid & 31;
   // stage 1: row tid = (t, b = lane) holds x[32a + b], a = 0..31
+  constexpr int NP = Parts<BF16>::n;
 #pragma unroll
   for (int kc = 0; kc < 8; ++kc) {
-    uint32_t h[4], l[4];
+    uint32_t p[4][NP];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) split2<BF16>(scale2(x(t, 32 * (4 * kc + j) + lane), sc1), h[j], l[j]);
-    *reinterpret_cast<uint4*>(s.a_hi + kmaj_off(tid, 8 * kc)) = make_uint4(h[0], h[1], h[2], h[3]);
-    *reinterpret_cast<uint4*>(s.a_lo + kmaj_off(tid, 8 * kc)) = make_uint4(l[0], l[1], l[2], l[3]);
+    for (int j = 0; j < 4; ++j) splitn<BF16>(scale2(x(t, 32 * (4 * kc + j) + lane), sc1), p[j]);
+#pragma unroll
+    for (int i = 0; i < NP; ++i)
+      *reinterpret_cast<uint4*>(s.a[i] + kmaj_off(tid, 8 * kc)) = make_uint4(p[0][i], p[1][i], p[2][i], p[3][i]);
   }
   return dft1024_stages<BF16>(s, phase, tid, y, mid, sc1, sc2);
 }
 
-// Copies the DFT-32 operand halves (logical [n][k] 64 x 64 16-bit arrays in
-// global memory) into the canonical layout.
-__device__ __forceinline__ void load_dft32_operand(char* b_hi, char* b_lo, const uint16_t* g_hi, const uint16_t* g_lo,
-                                                   int tid, int nthreads) {
+// Copies the DFT-32 operand parts (kMaxParts logical [n][k] 64 x 64 16-bit
+// arrays, one after the other in global memory) into the canonical layout.
+__device__ __forceinline__ void load_dft32_operand(char* const (&b)[kMaxParts], const uint16_t* g_parts, int tid,
+                                                   int nthreads) {
   for (int i = tid; i < 64 * 64; i += nthreads) {
     const int n = i >> 6, k = i & 63;
-    *reinterpret_cast<uint16_t*>(b_hi + kmaj_off(n, k)) = g_hi[i];
-    *reinterpret_cast<uint16_t*>(b_lo + kmaj_off(n, k)) = g_lo[i];
+#pragma unroll
+    for (int q = 0; q < kMaxParts; ++q) *reinterpret_cast<uint16_t*>(b[q] + kmaj_off(n, k)) = g_parts[q * 4096 + i];
   }
 }
 

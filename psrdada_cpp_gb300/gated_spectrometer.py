@@ -29,6 +29,7 @@ POWER, FULL_STOKES = 0, 1
 INTENDED, REFERENCE = 0, 1
 FLAG_SATURATION_RECORD = 1
 FLAG_NO_HOST_BUFFERS = 2
+FLAG_UNGATED = 4
 FORM_FP32, FORM_BF16, FORM_FP16 = 0, 1, 2
 TUNE_KEYS = ("tune_units", "tune_n1", "tune_scratch_mb")
 
@@ -351,6 +352,33 @@ class GatedSpectrometer:
 
     def last_error(self) -> str:
         return self._lib.gspec_last_error(self._h).decode()
+
+
+class FftSpectrometer(GatedSpectrometer):
+    """``FftSpectrometer<Handler>`` (``edd/FftSpectrometer.cuh:19-85``,
+    ``edd/detail/FftSpectrometer.cu:13-179``): the ungated spectrometer on
+    the same library (``GSPEC_FLAG_UNGATED``).  The block holds only packed
+    samples; every ``fft_length`` of them is one R2C frame; ``naccumulate``
+    frames add up to one power spectrum of ``fft_length/2 + 1`` float32
+    channels; an output block is ``n_out`` such spectra, handed to the handler
+    with the reference's pipeline delay (block n's spectra at call n + 3).
+    ``init`` forwards the header unchanged.
+
+    Three defects of the reference are not reproduced: its in-place R2C plan
+    reads each frame from ``fft_length`` floats apart but writes
+    ``fft_length/2 + 1`` complex values apart (``:54-56,103-107``), so frames
+    overwrite their successors' input; its power buffers are never zeroed, so
+    an output block also holds every second earlier block (``:133-147``); and
+    it derives the frame count from the float count divided by
+    ``2 * nchans`` (``:107``), dropping frames."""
+
+    def __init__(self, buffer_bytes: int, fft_length: int, naccumulate: int, nbits: int, input_level: float,
+                 output_level: float, handler, device: int = 0, flags: int = 0, tune: dict | None = None,
+                 form: int = 0):
+        layout = DadaBufferLayout(buffer_bytes, buffer_bytes, 0)
+        super().__init__(layout, 0, 0, fft_length, naccumulate, nbits, input_level, output_level, handler,
+                         input_type=SINGLE_POL, output_type=POWER, device=device, flags=flags | FLAG_UNGATED,
+                         tune=tune, form=form)
 
 
 def query(config: GspecConfig) -> GspecInfo:

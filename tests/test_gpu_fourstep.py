@@ -52,7 +52,10 @@ def test_fourstep_fp32_parity(name, spec, lost):
 
 # ------------------------------------------------------------ full geometry
 # form -> (max, rms) bound on the per-bin relative error with the 1 % floor
-FULL_TOL = {G.FORM_FP32: (SPEC_TOL, 1e-6), G.FORM_FP16: (1e-4, 1e-5), G.FORM_BF16: (1e-3, 1e-4)}
+FULL_TOL = {G.FORM_FP32: (SPEC_TOL, 1e-6), G.FORM_FP16: (1e-4, 1e-5), G.FORM_BF16: (1e-4, 1e-5)}
+# fractional baselines carried in from a previous block: half of every frame's
+# samples per gate is this fill value
+START_BASELINES = np.array([0.3718, -0.2093, 0.5807, -0.4411], np.float32)
 _ORACLE = {}
 
 
@@ -62,7 +65,7 @@ def _full_case(name):
     spec = synth.config3() if name == "c3" else synth.config2()
     blk = synth.make_block(spec, seed=2 if name == "c3" else 1, block_index=0, kind=name)
     cfg = oracle_config(spec, "intended")
-    states = [O.PolState() for _ in range(spec.npol)]
+    states = [O.PolState(START_BASELINES[2 * p], START_BASELINES[2 * p + 1]) for p in range(spec.npol)]
     res = O.process_block_chunked(blk, cfg, states, outputs_per_chunk=2)
     _ORACLE.clear()                      # one full-size case in host memory at a time
     _ORACLE[name] = (spec, blk, cfg, res, states)
@@ -78,6 +81,7 @@ def _run_device(spec, blk, form):
         info = gs.info()
         d_blk = torch.from_numpy(blk).cuda()
         d_out = torch.zeros(int(info.output_bytes), dtype=torch.uint8, device="cuda")
+        gs.set_baselines(START_BASELINES)
         gs.set_profiling(True)
         gs.run_block_device(d_blk.data_ptr(), d_out.data_ptr(), torch.cuda.current_stream().cuda_stream)
         torch.cuda.synchronize()

@@ -7,9 +7,9 @@ import psrdada_cpp_gb300 as G
 
 pytestmark = pytest.mark.gpu
 
-# BF16 hi+lo: the dropped lo*lo term and the FP32 accumulation leave ~1e-5 of
-# the spectrum's rms per bin; FP16 halves (11-bit mantissas) ~1e-7
-TOL = {G.FORM_BF16: 1e-4, G.FORM_FP16: 1e-5}
+# BF16 in three parts (bf16x6) and FP16 in two (11-bit mantissas) both leave
+# ~2^-22..2^-24 of the spectrum's rms per bin
+TOL = {G.FORM_BF16: 1e-5, G.FORM_FP16: 1e-5}
 
 
 def run_tc(x: np.ndarray, form: int) -> np.ndarray:
@@ -57,12 +57,11 @@ S = synth.StreamSpec
 # split-precision forms against the FP64 oracle: per-bin relative error (Stokes
 # products normalised by I, floor 1 % of the mean) within CHAIN_TOL (max) and
 # CHAIN_RMS (root mean square); counters, gate assignment and baselines
-# bit-exact as in the FP32 form.  A BF16 hi+lo operand keeps 2^-18 of its
-# value (8-bit mantissas), so each of the four DFT-32 stages adds ~1e-5 of the
-# spectrum's rms amplitude; a bin at the 1 % floor sees ~20x that in relative
-# power.  FP16 halves (11-bit mantissas) keep 2^-24: FP32-like.
-CHAIN_TOL = {G.FORM_BF16: 1e-3, G.FORM_FP16: 1e-4}
-CHAIN_RMS = {G.FORM_BF16: 1e-4, G.FORM_FP16: 1e-5}
+# bit-exact as in the FP32 form.  The BF16 form's operands are split in three
+# 8-bit parts (bf16x6) and the FP16 form's in two 11-bit parts: both keep
+# ~2^-22..2^-24 of each value through the four DFT-32 stages.
+CHAIN_TOL = {G.FORM_BF16: 1e-4, G.FORM_FP16: 1e-4}
+CHAIN_RMS = {G.FORM_BF16: 1e-5, G.FORM_FP16: 1e-5}
 TC_CASES = [
     # dual-pol 12-bit at 2^20 (both passes on the tensor cores), outliers at full scale
     ("d12_n2p20", S("d12_n2p20", 12, True, 6144, 1, 1 << 21, 1 << 20, 2, diode_period_heaps=64), "c3"),
