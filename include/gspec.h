@@ -190,6 +190,74 @@ int gspec_get_saturation(gspec_handle* h, uint64_t* out);
 int gspec_register_host(void* ptr, size_t bytes);
 int gspec_unregister_host(void* ptr);
 
+/* Synthetic DADA blocks generated on the device, the producer side of tests
+ * and benchmarks; replaces the reference's dummy_data_generator
+ * (psrdada_cpp/effelsberg/edd/src/dummy_data_generator.cu).
+ * GSPEC_DUMMY_TWO_TONE: that program's block (8 bit only): two tones from a
+ * C2R of 50 at bin nFreqs/3 and 20 at bin nFreqs/2 over the block's data
+ * samples, quantised between the block's minimum and maximum to 0..255 and
+ * shifted by -128 (:130-156); d_work holds 8 bytes of device memory for the
+ * range.  GSPEC_DUMMY_STREAM: seeded noise (sigma) plus a tone
+ * (tone_amplitude, tone_period samples per cycle) per pol, clipped to nbits,
+ * packed big-endian into the heap layout (dual-pol heaps and items alternate
+ * P0 P1), with the selected item of every heap carrying the diode state
+ * ((global heap / diode_period_heaps) & 1) in selected_bit and, for a
+ * lost_fraction of heaps, bit 63; block_index continues the stream. */
+#define GSPEC_DUMMY_TWO_TONE 0u
+#define GSPEC_DUMMY_STREAM 1u
+typedef struct gspec_dummy_config {
+  uint64_t buffer_size, heap_size, n_side_channels;
+  uint32_t nbits, dual_pol;
+  uint32_t mode, reserved;
+  uint64_t block_index, seed;
+  uint64_t selected_side_channel, selected_bit, diode_period_heaps;
+  uint64_t tone_period;
+  float sigma, tone_amplitude, lost_fraction, reserved2;
+} gspec_dummy_config;
+int gspec_dummy_block_device(const gspec_dummy_config* cfg, void* d_block, void* d_work, void* cuda_stream);
+/* The same block generated on the current device and copied into host memory
+ * (a convenience for producers: allocates and frees its device buffers). */
+int gspec_dummy_block(const gspec_dummy_config* cfg, void* host_block);
+
+/* VLBI: samples to 2-bit VDIF frames (replaces VLBI<Handler>,
+ * psrdada_cpp/effelsberg/edd/VLBI.cuh:91-170, edd/detail/VLBI.cu): the whole
+ * block is 8- or 12-bit samples; each block is quantised to 2 bits at
+ * -v sigma, 0, +v sigma about its mean (pack2bit_nonLinear,
+ * edd/src/VLBI.cu:183-237, with exact integer block statistics) and cut into
+ * VDIF frames of the template header's data frame length; frames_per_output
+ * (= 2-bit bytes per block / payload + 1) frames are handed out per call,
+ * those without data marked invalid, with the reference's delay (block n at
+ * call n + 3).  gspec_vlbi_init reads SYNC_TIME and SAMPLE_CLOCK_START from
+ * the DADA header (edd/detail/VLBI.cu:92-134): VDIF starts at the next whole
+ * second and the samples before it are dropped.  Status codes as gspec_process. */
+typedef struct gspec_vlbi gspec_vlbi;
+typedef struct gspec_vlbi_config {
+  uint64_t buffer_size;          /* bytes per input block (all samples) */
+  uint32_t nbits;                /* 8 or 12 */
+  int32_t device;
+  uint64_t spead_heap_size;      /* recorded only, as in the reference */
+  double sample_rate;            /* samples per second */
+  double digitizer_threshold;    /* v */
+  uint32_t vdif_header[8];       /* template: data frame length (8-byte units, header included), station,
+                                    thread, channels; epoch, second and frame number are set by init */
+} gspec_vlbi_config;
+typedef struct gspec_vlbi_info {
+  uint64_t frame_bytes, frames_per_output, output_bytes, frames_per_second, bytes_to_skip, spill_bytes;
+  uint32_t header[8];            /* the next frame's header */
+  int64_t last_sum;              /* integer sum and sum of squares of the last processed block */
+  uint64_t last_sum_sq;
+} gspec_vlbi_info;
+gspec_vlbi* gspec_vlbi_create(const gspec_vlbi_config* cfg, char* err, size_t err_len);
+int gspec_vlbi_init(gspec_vlbi* h, char* header, size_t total_bytes);
+int gspec_vlbi_process(gspec_vlbi* h, const char* block, size_t used_bytes, gspec_output* out);
+int gspec_vlbi_get_info(gspec_vlbi* h, gspec_vlbi_info* info);
+const char* gspec_vlbi_last_error(gspec_vlbi* h);
+void gspec_vlbi_destroy(gspec_vlbi* h);
+/* Sets a VDIF header's reference epoch (half-years since 2000) and seconds
+ * since the epoch from a POSIX time (VDIFHeader::setTimeReferencesFromTimestamp,
+ * edd/src/VLBI.cu:143-170); GSPEC_ERR_ARG before 2000. */
+int gspec_vdif_set_time(uint32_t* header, uint64_t posix_seconds);
+
 /* Allocation-free variant of gspec_run_block_device (no counterpart in the
  * reference).  For callers that cannot allocate device memory between blocks
  * (device memory reserved up front by a ring buffer or an outside pool,

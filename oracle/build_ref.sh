@@ -1,14 +1,16 @@
 #!/usr/bin/env bash
 # Builds oracle/_ref/libref_host.so from the reference's own sources where
-# they lie (psrdada_cpp tree, default /root/reference), with the stub headers
+# they lie (the psrdada_cpp tree given as the first argument or in
+# PSRDADA_CPP_TREE; without either it builds nothing), with the stub headers
 # in oracle/ref_shim/ standing in for googletest, Boost.Log and psrdada.
 # The library exports the reference's host-side C reference functions
 # (see oracle/ref_shim/ref_exports.cu); it is used only to pin the oracle.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${PSRDADA_CPP_TREE:-}}"
 OUT="$HERE/_ref"
 NVCC="${NVCC:-/usr/local/cuda/bin/nvcc}"
+if [ -z "$REF" ]; then echo "no psrdada_cpp tree given (argument or PSRDADA_CPP_TREE): reference pin not built"; exit 0; fi
 [ -d "$REF/psrdada_cpp" ] || { echo "reference tree not found at $REF" >&2; exit 2; }
 mkdir -p "$OUT"
 EDD="$REF/psrdada_cpp/effelsberg/edd"

@@ -532,6 +532,162 @@ def fft_spectrometer_block(block: np.ndarray, nbits: int, fft_length: int, naccu
 
 
 # --------------------------------------------------------------------------
+# Synthetic producer (edd/src/dummy_data_generator.cu)
+# --------------------------------------------------------------------------
+def dummy_two_tone_block(n: int) -> np.ndarray:
+    """The reference generator's data: the C2R (unnormalised) of 50 at bin
+    nFreqs/3 and 20 at bin nFreqs/2, nFreqs = n/2 + 1
+    (``dummy_data_generator.cu:130-137``), as float32; quantised between its
+    own minimum and maximum to 0..255 by ``packNbit<8>``
+    (``edd/Packer.cuh:32-41``: (x - min) / level, level = (max - min) / 255,
+    clamped, truncated) and shifted by -128 (``:150-156``).  int8 samples."""
+    t = np.arange(n, dtype=np.int64)
+    nf = n // 2 + 1
+    x = np.zeros(n)
+    for k, amp in ((nf // 3, 50.0), (nf // 2, 20.0)):
+        w = amp if (k == 0 or 2 * k == n) else 2.0 * amp
+        x += w * np.cos(2.0 * np.pi * ((k * t) % n) / n)
+    x = x.astype(np.float32)
+    lo, hi = x.min(), x.max()
+    level = np.float32((hi - lo) / np.float32(255.0))
+    v = np.clip((x - lo) / level, np.float32(0), np.float32(255)).astype(np.uint32)
+    return (v.astype(np.int32) - 128).astype(np.int8)
+
+
+def _mix64(z):
+    z = (z + np.uint64(0x9E3779B97F4A7C15)) & np.uint64(0xFFFFFFFFFFFFFFFF)
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def dummy_stream_samples(seed: int, pol: int, s0: int, n: int, sigma: float, tone_amplitude: float,
+                         tone_period: int, nbits: int) -> np.ndarray:
+    """Samples s0 .. s0+n-1 of one pol of the device generator's stream mode:
+    the centred sum of twelve 16-bit uniforms of a splitmix64 counter hash
+    times sigma / 65536, plus tone_amplitude cos(2 pi (s mod tone_period) /
+    tone_period), rounded half to even and clipped to nbits."""
+    with np.errstate(over="ignore"):
+        s = np.arange(s0, s0 + n, dtype=np.uint64)
+        key = _mix64(np.uint64(seed) ^ np.uint64(0x51ED27 * (pol + 1))) ^ s
+        tot = np.zeros(n, np.int64)
+        for j in range(3):
+            h = _mix64(key * np.uint64(3) + np.uint64(j))
+            for i in range(4):
+                tot += ((h >> np.uint64(16 * i)) & np.uint64(0xFFFF)).astype(np.int64)
+    noise = (tot - 393210).astype(np.float64) * float(np.float32(sigma)) / 65536.0
+    tone = 0.0
+    if tone_period > 0 and tone_amplitude != 0:
+        tone = float(np.float32(tone_amplitude)) * np.cos(2.0 * np.pi * (s.astype(np.int64) % tone_period) / tone_period)
+    lo, hi = -(1 << (nbits - 1)), (1 << (nbits - 1)) - 1
+    return np.clip(np.rint(noise + tone), lo, hi).astype(np.int64)
+
+
+# --------------------------------------------------------------------------
+# VLBI: 2-bit VDIF (edd/detail/VLBI.cu, edd/src/VLBI.cu)
+# --------------------------------------------------------------------------
+def vdif_time_fields(posix_seconds: int):
+    """(reference epoch, seconds since the epoch) of a POSIX time: epochs are
+    half-years since 2000-01-01 UTC (``VDIFHeader::setTimeReferencesFromTimestamp``,
+    ``edd/src/VLBI.cu:143-170``)."""
+    import datetime
+    t = datetime.datetime.fromtimestamp(posix_seconds, tz=datetime.timezone.utc)
+    half = 1 if t.month >= 7 else 0
+    start = datetime.datetime(t.year, 7 if half else 1, 1, tzinfo=datetime.timezone.utc)
+    return (t.year - 2000) * 2 + half, int((t - start).total_seconds())
+
+
+def vlbi_pack2bit(samples: np.ndarray, v: float) -> np.ndarray:
+    """``pack2bit_nonLinear`` (``edd/src/VLBI.cu:183-237``) with the block
+    statistics of ``edd/detail/VLBI.cu:216-237`` (mean, then the mean square
+    residual): level = (x - mean >= -v sigma) + (x - mean >= 0) +
+    (x - mean >= v sigma), four samples per byte, sample j in bits 2j..2j+1.
+    The sums are exact integers here (the reference adds floats in a
+    nondeterministic order); mean and sigma^2 in FP64, rounded to float."""
+    x = np.asarray(samples, np.int64)
+    n = x.size
+    mean_d = float(x.sum()) / n
+    var = float((x * x).sum()) / n - mean_d * mean_d
+    mean = np.float32(mean_d)
+    vsig = np.float32(np.float32(v) * np.sqrt(np.float32(max(var, 0.0))))
+    inp = x.astype(np.float32) - mean
+    lev = ((inp >= -vsig).astype(np.uint8) + (inp >= 0).astype(np.uint8) + (inp >= vsig).astype(np.uint8))
+    lev = lev.reshape(-1, 4)
+    return (lev[:, 0] | (lev[:, 1] << 2) | (lev[:, 2] << 4) | (lev[:, 3] << 6)).astype(np.uint8)
+
+
+class OracleVLBI:
+    """``VLBI<Handler>`` (``edd/detail/VLBI.cu:22-354``) on the CPU: block n's
+    frames are handed out at call n + 3; the 2-bit stream of a block is
+    [spill of the previous block | the block's bytes after the first-second
+    skip]; every output holds ``frames_per_output`` frames, those without
+    data invalid (the reference marks the validity one frame late, a defect
+    not reproduced)."""
+
+    def __init__(self, buffer_size, nbits, sample_rate, v, header_words):
+        self.buffer_size, self.nbits, self.rate, self.v = buffer_size, nbits, sample_rate, v
+        self.hdr = [int(w) & 0xFFFFFFFF for w in header_words]
+        self.hdr[3] = (self.hdr[3] & ~(0x1F << 26)) | (1 << 26)
+        self.hdr[3] &= ~(1 << 31)
+        self.frame_bytes = (self.hdr[2] & 0xFFFFFF) * 8
+        self.payload = self.frame_bytes - 32
+        self.nsamples = buffer_size * 8 // nbits
+        self.packed = self.nsamples // 4
+        self.nframes = self.packed // self.payload + 1
+        self.fps = int(sample_rate / (self.payload * 4))
+        self.skip = 0
+        self.spill = b""
+        self.pending = []        # outputs awaiting hand-out
+        self.calls = 0
+        self.last = None
+
+    def init(self, sync_time, sample_clock_start):
+        frac = sync_time + sample_clock_start / self.rate
+        ts = int(frac) + 1
+        self.skip = int((ts - frac) * self.rate) * 2 // 8
+        ep, sec = vdif_time_fields(ts)
+        self.hdr[1] = (self.hdr[1] & ~(0x3F << 24)) | (ep << 24)
+        self.hdr[0] = (self.hdr[0] & ~0x3FFFFFFF) | sec
+
+    def _frames(self, block):
+        packed = vlbi_pack2bit(unpack(np.asarray(block, np.uint8), self.nbits), self.v).tobytes()
+        stream = self.spill + packed[self.skip:]
+        self.skip = 0
+        nvalid = len(stream) // self.payload
+        out = bytearray(self.nframes * self.frame_bytes)
+        num0, sec0 = self.hdr[1] & 0xFFFFFF, self.hdr[0] & 0x3FFFFFFF
+        for f in range(self.nframes):
+            num = num0 + f
+            w = list(self.hdr)
+            w[0] = (w[0] & ~0x3FFFFFFF) | ((sec0 + num // self.fps) & 0x3FFFFFFF)
+            w[0] = (w[0] & ~(1 << 31)) | ((0 if f < nvalid else 1) << 31)
+            w[1] = (w[1] & ~0xFFFFFF) | (num % self.fps)
+            o = f * self.frame_bytes
+            out[o:o + 32] = np.array(w, "<u4").tobytes()
+            if f < nvalid:
+                out[o + 32:o + self.frame_bytes] = stream[f * self.payload:(f + 1) * self.payload]
+        self.spill = stream[nvalid * self.payload:]
+        num = num0 + nvalid
+        self.hdr[1] = (self.hdr[1] & ~0xFFFFFF) | (num % self.fps)
+        self.hdr[0] = (self.hdr[0] & ~0x3FFFFFFF) | ((sec0 + num // self.fps) & 0x3FFFFFFF)
+        return bytes(out)
+
+    def __call__(self, block):
+        """(stop, frames handed out or None)."""
+        if self.skip > self.packed:
+            self.skip -= self.packed
+            return False, None
+        if len(block) != self.buffer_size:
+            return True, None
+        self.calls += 1
+        self.pending.append(self._frames(block))
+        # handed out three calls after the block arrived
+        if self.calls >= 4:
+            return False, self.pending.pop(0)
+        return False, None
+
+
+# --------------------------------------------------------------------------
 # R13 / R14: output block layout
 # --------------------------------------------------------------------------
 def output_bytes(spectra: np.ndarray, n0: np.ndarray, n1: np.ndarray, dual_pol: bool) -> bytes:

@@ -17,7 +17,8 @@ LIB = Path(os.environ["GSPEC_LIB"]) if os.environ.get("GSPEC_LIB") else PKG / "l
 # extra nvcc flags (e.g. -D tuning knobs) and a separate object folder for variant builds
 EXTRA = os.environ.get("GSPEC_NVCC_FLAGS", "").split()
 SOURCES = ["gspec_kernels.cu", "gspec_fourstep.cu", "gspec_engine.cu", "gspec_noalloc.cu", "gspec_server.cu",
-           "gspec_batch.cu", "gspec_tc.cu"]
+           "gspec_batch.cu", "gspec_tc.cu", "gspec_dummy.cu",
+           "gspec_vlbi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 

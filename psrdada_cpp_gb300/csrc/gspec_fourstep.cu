@@ -311,13 +311,11 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, GSPEC_PASSB_MINB)
     }
     __syncthreads();
   }
-  // bin 0 from the exact per-job sums (exact_dc), over the jobs in order
-  if (rp == 0 && tid == 0) {
-    float d[VALS];
-    exact_dc_bin<DUAL>(p, k, d);
-#pragma unroll
-    for (int v = 0; v < VALS; ++v) acc[0][v] = d[v];
-  }
+  // bin 0 from the exact per-job sums (exact_dc), over the jobs in order;
+  // the work buffer is free after the loop's last barrier
+  if (rp == 0)
+    exact_dc_bin<DUAL>(p, k, reinterpret_cast<float*>(work),
+                       static_cast<uint32_t>(Cfg::WORK_BYTES / (VALS * sizeof(float))), acc[0]);
   // gates without data: constant baseline in bin 0 (row pair 0, slot a = 0)
   if (rp == 0 && tid == 0) {
     const float n = static_cast<float>(N);

@@ -160,15 +160,37 @@ __device__ __forceinline__ float2 exact_dc(const FourStepParams& p, uint32_t k, 
 
 // The sums of bin 0 (slot 0 of row pair 0) recomputed from the exact DC of
 // every job of output spectrum k, in job order (replacing the FFT's bin 0).
+// Every thread of the row-pair-0 CTA calls it (it contains barriers): each
+// job's contribution is formed by one thread into `scratch` (at most `cap`
+// jobs at a time) and thread 0 adds them into acc0 in job order, which gives
+// the same sums as adding the jobs one after the other.
 template <bool DUAL, int VALS>
-__device__ __noinline__ void exact_dc_bin(const FourStepParams& p, uint32_t k, float (&acc)[VALS]) {
-#pragma unroll
-  for (int v = 0; v < VALS; ++v) acc[v] = 0.f;
+__device__ __forceinline__ void exact_dc_bin(const FourStepParams& p, uint32_t k, float* scratch, uint32_t cap,
+                                             float (&acc0)[VALS]) {
   const uint32_t nj = p.njobs[k];
-  for (uint32_t j = 0; j < nj; ++j) {
-    const uint32_t job = p.jobs[k * p.maxjobs + j];
-    const float2 z = exact_dc(p, k, j, job, DUAL);
-    accumulate_bin<DUAL>(acc, z, z, job);
+  const uint32_t tid = threadIdx.x;
+  if (tid == 0) {
+#pragma unroll
+    for (int v = 0; v < VALS; ++v) acc0[v] = 0.f;
+  }
+  for (uint32_t j0 = 0; j0 < nj; j0 += cap) {
+    const uint32_t n = min(cap, nj - j0);
+    for (uint32_t t = tid; t < n; t += blockDim.x) {
+      float c[VALS];
+#pragma unroll
+      for (int v = 0; v < VALS; ++v) c[v] = 0.f;
+      const uint32_t job = p.jobs[k * p.maxjobs + j0 + t];
+      const float2 z = exact_dc(p, k, j0 + t, job, DUAL);
+      accumulate_bin<DUAL>(c, z, z, job);
+#pragma unroll
+      for (int v = 0; v < VALS; ++v) scratch[t * VALS + v] = c[v];
+    }
+    __syncthreads();
+    if (tid == 0)
+      for (uint32_t t = 0; t < n; ++t)
+#pragma unroll
+        for (int v = 0; v < VALS; ++v) acc0[v] += scratch[t * VALS + v];
+    __syncthreads();
   }
 }
 

@@ -331,8 +331,7 @@ struct PassBLayout {
   static constexpr size_t A = 0;                     // operand parts; the transformed rows ("work") alias them
   static constexpr size_t B = Parts<BF16>::n * kABytes;   // [B1 | B2 | B3 | W1024]: the image
   static constexpr size_t W = B + kMaxParts * kBBytes;
-  static constexpr size_t STAGE = W + 1024 * sizeof(float2);
-  static constexpr size_t JW = STAGE + static_cast<size_t>(J) * 2 * 1024 * sizeof(float2);
+  static constexpr size_t JW = W + 1024 * sizeof(float2);
   static constexpr size_t BAR = JW + 16;
   static constexpr size_t BYTES = BAR + 32;
   static_assert(static_cast<size_t>(4) * kRowStride * sizeof(float2) <= Parts<BF16>::n * kABytes,
@@ -340,8 +339,11 @@ struct PassBLayout {
 };
 
 // grid.x = nk * N1/2: unit (output spectrum k, row pair rp); jobs two at a
-// time: their rows arrive by one TMA bulk-copy stage, which is refilled for
-// the next group as soon as the first DFT stage has read it.
+// time.  The first DFT stage reads its operand rows straight from the
+// scratch (a warp's loads cover 32 consecutive points of a row), and the next
+// group's rows are prefetched into L2 as soon as the first stage has read
+// the current ones; without a staging buffer in shared memory two CTAs fit
+// an SM in both forms.
 template <bool DUAL, bool BF16>
 __global__ void __launch_bounds__(kPassThreads, 2) tc_b_kernel(FourStepParams p) {
   constexpr int N2 = 1024;
@@ -355,12 +357,10 @@ __global__ void __launch_bounds__(kPassThreads, 2) tc_b_kernel(FourStepParams p)
     s.b[q] = smem + L::B + q * kBBytes;
   }
   float2* work = reinterpret_cast<float2*>(smem + L::A);
-  float2* stage = reinterpret_cast<float2*>(smem + L::STAGE);
   float2* w = reinterpret_cast<float2*>(smem + L::W);
   uint32_t* jw = reinterpret_cast<uint32_t*>(smem + L::JW);
-  uint64_t* tma_bar = reinterpret_cast<uint64_t*>(smem + L::BAR);
-  uint64_t* mma_bar = tma_bar + 1;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tma_bar + 2);
+  uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + L::BAR);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_bar + 2);
   s.w = w;
   s.bar = mma_bar;
 
@@ -379,7 +379,6 @@ __global__ void __launch_bounds__(kPassThreads, 2) tc_b_kernel(FourStepParams p)
   const uint32_t ngroups = (njobs + J - 1) / J;
 
   if (tid == 0) {
-    mbar_init(tma_bar, 1);
     mbar_init(mma_bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -390,19 +389,20 @@ __global__ void __launch_bounds__(kPassThreads, 2) tc_b_kernel(FourStepParams p)
   fence_after();
   s.tmem = *tmem_slot;
 
-  // thread 0: rows of job group g into the stage
-  auto issue = [&](uint32_t g) {
+  // the rows of job group g: transform t = 2 qq + r is row rowA (r = 0) or
+  // rowB (r = 1) of job g J + qq (the group's last job stands in for a missing one)
+  auto row_of = [&](uint32_t g, int t) {
     const uint32_t nq = min(static_cast<uint32_t>(J), njobs - g * J);
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    mbar_expect_tx(tma_bar, nq * 2 * kRowBytes);
-    for (uint32_t qq = 0; qq < nq; ++qq) {
-      const float2* seq = p.scratch + (static_cast<size_t>(kk) * p.maxjobs + g * J + qq) * N;
-      float2* dst = stage + qq * 2 * N2;
-      bulk_g2s(dst, seq + static_cast<size_t>(rowA) * N2, kRowBytes, tma_bar);
-      bulk_g2s(dst + N2, seq + static_cast<size_t>(rowB) * N2, kRowBytes, tma_bar);
-    }
+    const uint32_t qq = min(static_cast<uint32_t>(t >> 1), nq - 1);
+    const float2* seq = p.scratch + (static_cast<size_t>(kk) * p.maxjobs + g * J + qq) * N;
+    return seq + static_cast<size_t>((t & 1) ? rowB : rowA) * N2;
   };
-  if (tid == 0 && ngroups > 0) issue(0);
+  // thread 0: group g's rows into L2
+  auto prefetch = [&](uint32_t g) {
+    for (int t = 0; t < 2 * J; ++t)
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(row_of(g, t)), "r"(kRowBytes) : "memory");
+  };
+  if (tid == 0 && ngroups > 0) prefetch(0);
 
   // job words one group ahead: the global load of group g + 1 is in flight
   // while group g is transformed
@@ -416,24 +416,16 @@ __global__ void __launch_bounds__(kPassThreads, 2) tc_b_kernel(FourStepParams p)
   uint32_t phase = 0;
   bool mma_ok = true;
   for (uint32_t g = 0; g < ngroups; ++g) {
-    const bool ok = mbar_wait(tma_bar, g & 1u, 1u << 24);
-    if (__syncthreads_or(!ok)) {
-      if (tid == 0) {
-        if (p.c.dev_err) atomicExch(p.c.dev_err, 2u);
-        mbar_wait(tma_bar, g & 1u, 1u << 20);   // a bounded chance for the copies in flight to land
-      }
-      __syncthreads();
-      break;
-    }
     const uint32_t j0 = g * J;
     const int nq = static_cast<int>(min(static_cast<uint32_t>(J), njobs - j0));
     if (tid < nq) jw[tid] = next_job;
     if (tid < J && j0 + J + tid < njobs) next_job = jobs[j0 + J + tid];
+    const float2* my_row = row_of(g, tid >> 5);
     mma_ok = dft1024_tile<BF16>(
-                 s, phase, tid, [&](int t, int n) { return stage[t * N2 + n]; },
+                 s, phase, tid, [&](int, int n) { return __ldg(my_row + n); },
                  [&](int t, int k2, float2 v) { work[t * kRowStride + spad(k2)] = v; },
                  [&] {
-                   if (tid == 0 && g + 1 < ngroups) issue(g + 1);
+                   if (tid == 0 && g + 1 < ngroups) prefetch(g + 1);
                  },
                  Scales<BF16>::b1, Scales<BF16>::b2) &&
              mma_ok;
@@ -454,13 +446,11 @@ __global__ void __launch_bounds__(kPassThreads, 2) tc_b_kernel(FourStepParams p)
     __syncthreads();
   }
   if (!mma_ok && tid == 0 && p.c.dev_err) atomicExch(p.c.dev_err, 3u);
-  // bin 0 from the exact per-job sums (exact_dc), over the jobs in order
-  if (rp == 0 && tid == 0) {
-    float d[VALS];
-    exact_dc_bin<DUAL>(p, k, d);
-#pragma unroll
-    for (int v = 0; v < VALS; ++v) acc[0][v] = d[v];
-  }
+  // bin 0 from the exact per-job sums (exact_dc), over the jobs in order;
+  // the operand buffers are free after the loop's last barrier
+  if (rp == 0)
+    exact_dc_bin<DUAL>(p, k, reinterpret_cast<float*>(smem + L::A),
+                       static_cast<uint32_t>(Parts<BF16>::n * kABytes / (VALS * sizeof(float))), acc[0]);
   // gates without data: constant baseline in bin 0 (row pair 0, slot a = 0)
   if (rp == 0 && tid == 0) {
     const float n = static_cast<float>(N);

@@ -52,7 +52,7 @@ constexpr uint32_t kImageBytes = kMaxParts * kBBytes + 1024 * 8;   // [B1 | B2 |
 static_assert(kImageBytes == 3 * 9216 + 1024 * 8, "image size as declared for the host");
 
 #ifndef GSPEC_BF16_PRODUCTS
-#define GSPEC_BF16_PRODUCTS 5
+#define GSPEC_BF16_PRODUCTS 6
 #endif
 static_assert(GSPEC_BF16_PRODUCTS == 5 || GSPEC_BF16_PRODUCTS == 6, "BF16 split: 5 or 6 partial products");
 
