@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(128) dft1024_test_kernel(const float2* __restr
   fence_after();
   s.tmem = *tmem_slot;
   uint32_t phase = 0;
-  const bool ok = dft1024_tile<BF16>(
+  const bool ok = dft1024_tile<Split<BF16>>(
       s, phase, tid, [&](int t, int n) { return xs[t * 1024 + n]; },
       [&](int t, int k, float2 v) { out[(static_cast<size_t>(blockIdx.x) * 4 + t) * 1024 + k] = v; }, [] {});
   if (!ok && err) atomicExch(err, 3u);
@@ -171,6 +171,14 @@ constexpr int kRowStride = spad_size(1024);
 // FP16 operand scales (powers of two): pass A inputs are at most 2^11 in
 // magnitude, its stage-1 outputs at most 2^11 * 32 * sqrt(2); pass B inputs
 // (pass A outputs) at most 2^11 * 1024 * sqrt(2).
+// split of each pass: the column pass's first stage transforms integer
+// samples, which two parts hold exactly (5 products in BF16); the row pass
+// transforms general values (bf16x6 in BF16)
+template <bool BF16>
+using SplitA = Split<BF16, 2>;
+template <bool BF16>
+using SplitB = Split<BF16, BF16 ? 3 : 2>;
+
 template <bool BF16> struct Scales {
   static constexpr float a1 = 1.f, a2 = BF16 ? 1.f : 0.25f;
   static constexpr float b1 = BF16 ? 1.f : 1.f / 64, b2 = BF16 ? 1.f : 1.f / 32;
@@ -186,7 +194,7 @@ struct PassALayout {
   static constexpr int BC = 8;                          // columns per CTA: two tiles of 4
   static constexpr int THREADS = 2 * kPassThreads;      // one 128-thread group per tile
   static constexpr size_t A = 0;                        // per tile: operand parts, then its transformed columns
-  static constexpr size_t TILE = Parts<BF16>::n * kABytes;
+  static constexpr size_t TILE = SplitA<BF16>::n * kABytes;
   static constexpr size_t B = 2 * TILE;                 // [B1 | B2 | B3 | W1024]: the image
   static constexpr size_t RED = B + kImageBytes;
   static constexpr size_t BAR = RED + (THREADS / 32) * 12 * 8;
@@ -201,7 +209,7 @@ struct PassALayout {
 // transformed columns (written over the operands) leave with the
 // W_N^(n2*k1) twiddle.
 template <int NBITS, bool DUAL, bool BF16>
-__global__ void __launch_bounds__(PassALayout<BF16>::THREADS, Parts<BF16>::n == 3 ? 1 : 2) tc_a_kernel(FourStepParams p) {
+__global__ void __launch_bounds__(PassALayout<BF16>::THREADS, SplitA<BF16>::n == 3 ? 1 : 2) tc_a_kernel(FourStepParams p) {
   constexpr int N1 = 1024;
   using L = PassALayout<BF16>;
   constexpr int BC = L::BC, THREADS = L::THREADS;
@@ -216,7 +224,7 @@ __global__ void __launch_bounds__(PassALayout<BF16>::THREADS, Parts<BF16>::n == 
   auto tile_smem = [&](int g) {
     TileSmem t;
     for (int q = 0; q < kMaxParts; ++q) {
-      t.a[q] = smem + L::A + g * L::TILE + (q < Parts<BF16>::n ? q : 0) * kABytes;
+      t.a[q] = smem + L::A + g * L::TILE + (q < SplitA<BF16>::n ? q : 0) * kABytes;
       t.b[q] = smem + L::B + q * kBBytes;
     }
     t.w = reinterpret_cast<const float2*>(smem + L::B + kMaxParts * kBBytes);
@@ -286,7 +294,7 @@ __global__ void __launch_bounds__(PassALayout<BF16>::THREADS, Parts<BF16>::n == 
 #pragma unroll
     for (int e = 0; e < SP; ++e) {
       const int col = e - keep0;
-      if (col >= 0 && col < BC) put_stage1<BF16>(col < 4 ? s0 : s1, col & 3, n1, make_float2(re[e], im[e]), sc1);
+      if (col >= 0 && col < BC) put_stage1<SplitA<BF16>>(col < 4 ? s0 : s1, col & 3, n1, make_float2(re[e], im[e]), sc1);
     }
   }
   fence_before();
@@ -295,7 +303,7 @@ __global__ void __launch_bounds__(PassALayout<BF16>::THREADS, Parts<BF16>::n == 
   s.tmem = *tmem_slot + grp * kTmemCols;
   uint32_t phase = 0;
   float2* S = reinterpret_cast<float2*>(s.a[0]);          // this tile's columns after the transform
-  const bool ok = dft1024_stages<BF16>(
+  const bool ok = dft1024_stages<SplitA<BF16>>(
       s, phase, gtid, [&](int t, int k1, float2 v) { S[t * kColStride + spad(k1)] = v; }, [] {}, sc1, sc2);
   if (!ok && gtid == 0 && p.c.dev_err) atomicExch(p.c.dev_err, 3u);
   __syncthreads();
@@ -329,12 +337,12 @@ struct PassBLayout {
   static constexpr int VALS = DUAL ? 8 : 2;
   static constexpr int BPT = (1024 + 1 + kPassThreads - 1) / kPassThreads;
   static constexpr size_t A = 0;                     // operand parts; the transformed rows ("work") alias them
-  static constexpr size_t B = Parts<BF16>::n * kABytes;   // [B1 | B2 | B3 | W1024]: the image
+  static constexpr size_t B = SplitB<BF16>::n * kABytes;   // [B1 | B2 | B3 | W1024]: the image
   static constexpr size_t W = B + kMaxParts * kBBytes;
   static constexpr size_t JW = W + 1024 * sizeof(float2);
   static constexpr size_t BAR = JW + 16;
   static constexpr size_t BYTES = BAR + 32;
-  static_assert(static_cast<size_t>(4) * kRowStride * sizeof(float2) <= Parts<BF16>::n * kABytes,
+  static_assert(static_cast<size_t>(4) * kRowStride * sizeof(float2) <= SplitB<BF16>::n * kABytes,
                 "work fits the operands");
 };
 
@@ -353,7 +361,7 @@ __global__ void __launch_bounds__(kPassThreads, 2) tc_b_kernel(FourStepParams p)
   extern __shared__ __align__(1024) char smem[];
   TileSmem s;
   for (int q = 0; q < kMaxParts; ++q) {
-    s.a[q] = smem + L::A + (q < Parts<BF16>::n ? q : 0) * kABytes;
+    s.a[q] = smem + L::A + (q < SplitB<BF16>::n ? q : 0) * kABytes;
     s.b[q] = smem + L::B + q * kBBytes;
   }
   float2* work = reinterpret_cast<float2*>(smem + L::A);
@@ -421,7 +429,7 @@ __global__ void __launch_bounds__(kPassThreads, 2) tc_b_kernel(FourStepParams p)
     if (tid < nq) jw[tid] = next_job;
     if (tid < J && j0 + J + tid < njobs) next_job = jobs[j0 + J + tid];
     const float2* my_row = row_of(g, tid >> 5);
-    mma_ok = dft1024_tile<BF16>(
+    mma_ok = dft1024_tile<SplitB<BF16>>(
                  s, phase, tid, [&](int, int n) { return __ldg(my_row + n); },
                  [&](int t, int k2, float2 v) { work[t * kRowStride + spad(k2)] = v; },
                  [&] {
@@ -450,7 +458,7 @@ __global__ void __launch_bounds__(kPassThreads, 2) tc_b_kernel(FourStepParams p)
   // the operand buffers are free after the loop's last barrier
   if (rp == 0)
     exact_dc_bin<DUAL>(p, k, reinterpret_cast<float*>(smem + L::A),
-                       static_cast<uint32_t>(Parts<BF16>::n * kABytes / (VALS * sizeof(float))), acc[0]);
+                       static_cast<uint32_t>(SplitB<BF16>::n * kABytes / (VALS * sizeof(float))), acc[0]);
   // gates without data: constant baseline in bin 0 (row pair 0, slot a = 0)
   if (rp == 0 && tid == 0) {
     const float n = static_cast<float>(N);

@@ -13,16 +13,16 @@
 // whose parts together carry the leading bits:
 //   FP16 (11-bit parts, two per operand): A1 B1 + A1 B2 + A2 B1, 12 MMAs of
 //     K = 16 per stage; what is left is ~2^-22 of the result;
-//   BF16 (8-bit parts), GSPEC_BF16_PRODUCTS = 6: three parts per operand and
-//     the bf16x6 scheme of Henry, Tang and Heinecke ("Leveraging the bfloat16
-//     artificial intelligence datatype for higher-precision computations",
-//     ARITH 2019): A1 B1 + A1 B2 + A2 B1 + A2 B2 + A1 B3 + A3 B1, 24 MMAs per
-//     stage, ~2^-24 left over;
-//   BF16, GSPEC_BF16_PRODUCTS = 5: the data operand A in two parts, the
-//     constant DFT-32 matrix B in three, A1 B1 + A1 B2 + A2 B1 + A2 B2 +
-//     A1 B3 (20 MMAs): of the three 2^-18 terms of the two-part split (A's
-//     remainder, B's remainder, A2 B2) only A's remainder is left, and the
-//     operand build and shared memory are those of the two-part split.
+//   BF16 (8-bit parts), three parts per operand: the bf16x6 scheme of Henry,
+//     Tang and Heinecke ("Leveraging the bfloat16 artificial intelligence
+//     datatype for higher-precision computations", ARITH 2019):
+//     A1 B1 + A1 B2 + A2 B1 + A2 B2 + A1 B3 + A3 B1, 24 MMAs per stage,
+//     ~2^-24 left over;
+//   BF16 with the data operand A in two parts and the constant DFT-32 matrix
+//     B in three: A1 B1 + A1 B2 + A2 B1 + A2 B2 + A1 B3 (20 MMAs): exact for
+//     data that two parts hold exactly (integer samples up to 2^16), else
+//     A's remainder (~2^-18) is left.  The column pass uses it (its first
+//     stage transforms integer samples), the row pass uses bf16x6.
 // The small products are issued first so that they are summed before the
 // large one joins the accumulator.
 //
@@ -51,16 +51,17 @@ constexpr int kMaxParts = 3;
 constexpr uint32_t kImageBytes = kMaxParts * kBBytes + 1024 * 8;   // [B1 | B2 | B3 | W1024] in shared-memory layout
 static_assert(kImageBytes == 3 * 9216 + 1024 * 8, "image size as declared for the host");
 
-#ifndef GSPEC_BF16_PRODUCTS
-#define GSPEC_BF16_PRODUCTS 6
-#endif
-static_assert(GSPEC_BF16_PRODUCTS == 5 || GSPEC_BF16_PRODUCTS == 6, "BF16 split: 5 or 6 partial products");
-
-// parts of the data operand A (n) and partial products of a stage (products)
-template <bool BF16>
-struct Parts {
-  static constexpr int n = BF16 ? (GSPEC_BF16_PRODUCTS == 6 ? 3 : 2) : 2;
-  static constexpr int products = BF16 ? GSPEC_BF16_PRODUCTS : 3;
+// Split policy of one pass: the 16-bit type, the parts of the data operand
+// A (n) and the partial products of a stage.  FP16: two parts, 3 products.
+// BF16 with n = 3: bf16x6 (6 products); with n = 2 (data exact in two
+// parts, e.g. integer samples): A1 B1 + A1 B2 + A2 B1 + A2 B2 + A1 B3
+// (5 products).  The DFT-32 matrix B has three parts in BF16, two in FP16.
+template <bool BF16_, int NPA_ = (BF16_ ? 3 : 2)>
+struct Split {
+  static constexpr bool bf16 = BF16_;
+  static constexpr int n = NPA_;
+  static constexpr int products = !BF16_ ? 3 : (NPA_ == 3 ? 6 : 5);
+  static_assert(BF16_ ? (NPA_ == 2 || NPA_ == 3) : NPA_ == 2, "parts of the form");
 };
 constexpr uint32_t kWaitLimit = 1u << 22;
 
@@ -123,14 +124,14 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// Split of a complex value into Parts<BF16>::n packed 16-bit pairs (re in
-// the low half): part i is the rounding of what parts 0..i-1 left; every
-// remainder is exact in FP32.
-template <bool BF16>
-__device__ __forceinline__ void splitn(float2 v, uint32_t (&p)[Parts<BF16>::n]) {
+// Split of a complex value into SP::n packed 16-bit pairs (re in the low
+// half): part i is the rounding of what parts 0..i-1 left; every remainder
+// is exact in FP32.
+template <class SP>
+__device__ __forceinline__ void splitn(float2 v, uint32_t (&p)[SP::n]) {
 #pragma unroll
-  for (int i = 0; i < Parts<BF16>::n; ++i) {
-    if constexpr (BF16) {
+  for (int i = 0; i < SP::n; ++i) {
+    if constexpr (SP::bf16) {
       const __nv_bfloat162 h = __floats2bfloat162_rn(v.x, v.y);
       const float2 hf = __bfloat1622float2(h);
       p[i] = *reinterpret_cast<const uint32_t*>(&h);
@@ -146,7 +147,7 @@ __device__ __forceinline__ void splitn(float2 v, uint32_t (&p)[Parts<BF16>::n]) 
 
 // Shared memory of one tile engine (offsets from a 1024-byte aligned base).
 struct TileSmem {
-  char* a[kMaxParts];   // operand parts, kABytes each (the form uses Parts<BF16>::n)
+  char* a[kMaxParts];   // operand parts, kABytes each (the pass uses SP::n)
   char* b[kMaxParts];   // DFT-32 matrix parts, kBBytes each
   const float2* w;      // 1024 twiddles W1024^j
   uint64_t* bar;        // MMA completion barrier
@@ -154,31 +155,31 @@ struct TileSmem {
 };
 
 // (A part, B part) of the partial products of a stage, smallest first:
-// BF16 x6 (2,0) (0,2) (1,1) (1,0) (0,1) (0,0); BF16 x5 (1,1) (0,2) (1,0)
-// (0,1) (0,0); FP16 (1,0) (0,1) (0,0).
-template <bool BF16>
+// 6 products (2,0) (0,2) (1,1) (1,0) (0,1) (0,0); 5 products (1,1) (0,2)
+// (1,0) (0,1) (0,0); 3 products (1,0) (0,1) (0,0).
+template <class SP>
 __host__ __device__ constexpr int prod_a(int q) {
-  return !BF16 ? (q == 0 ? 1 : 0)
-               : Parts<true>::products == 6 ? (q == 0 ? 2 : q == 2 ? 1 : q == 3 ? 1 : 0)
-                                             : (q == 0 ? 1 : q == 2 ? 1 : 0);
+  return SP::products == 6 ? (q == 0 ? 2 : q == 2 ? 1 : q == 3 ? 1 : 0)
+         : SP::products == 5 ? (q == 0 ? 1 : q == 2 ? 1 : 0)
+                             : (q == 0 ? 1 : 0);
 }
-template <bool BF16>
+template <class SP>
 __host__ __device__ constexpr int prod_b(int q) {
-  return !BF16 ? (q == 1 ? 1 : 0)
-               : Parts<true>::products == 6 ? (q == 1 ? 2 : q == 2 ? 1 : q == 4 ? 1 : 0)
-                                             : (q == 0 ? 1 : q == 1 ? 2 : q == 3 ? 1 : 0);
+  return SP::products == 6 ? (q == 1 ? 2 : q == 2 ? 1 : q == 4 ? 1 : 0)
+         : SP::products == 5 ? (q == 0 ? 1 : q == 1 ? 2 : q == 3 ? 1 : 0)
+                             : (q == 1 ? 1 : 0);
 }
 
-// Issues one stage (the form's partial products over K = 64, 4 MMAs of
+// Issues one stage (the pass's partial products over K = 64, 4 MMAs of
 // K = 16 each, the smallest products first) and a commit.
-template <bool BF16>
+template <class SP>
 __device__ __forceinline__ void issue_stage(const TileSmem& s) {
-  constexpr uint32_t id = idesc(128, 64, BF16);
-  constexpr int NPROD = Parts<BF16>::products;
+  constexpr uint32_t id = idesc(128, 64, SP::bf16);
+  constexpr int NPROD = SP::products;
   fence_after();
 #pragma unroll
   for (int q = 0; q < NPROD; ++q) {
-    const uint32_t a = smem_addr(s.a[prod_a<BF16>(q)]), b = smem_addr(s.b[prod_b<BF16>(q)]);
+    const uint32_t a = smem_addr(s.a[prod_a<SP>(q)]), b = smem_addr(s.b[prod_b<SP>(q)]);
 #pragma unroll
     for (uint32_t ks = 0; ks < 4; ++ks) {
       const uint32_t off = ks * 2 * kLBO;
@@ -192,25 +193,25 @@ __device__ __forceinline__ float2 scale2(float2 v, float f) { return make_float2
 
 // Stage-1 operand of input x[t][n] (n = 32a + b) in row 32t + b, K = 2a + r,
 // stored by whoever produces the value (scaled by sc1, split hi/lo).
-template <bool BF16>
+template <class SP>
 __device__ __forceinline__ void put_stage1(const TileSmem& s, int t, int n, float2 v, float sc1) {
-  uint32_t p[Parts<BF16>::n];
-  splitn<BF16>(scale2(v, sc1), p);
+  uint32_t p[SP::n];
+  splitn<SP>(scale2(v, sc1), p);
   const uint32_t off = kmaj_off(32 * t + (n & 31), 2 * (n >> 5));
 #pragma unroll
-  for (int i = 0; i < Parts<BF16>::n; ++i) *reinterpret_cast<uint32_t*>(s.a[i] + off) = p[i];
+  for (int i = 0; i < SP::n; ++i) *reinterpret_cast<uint32_t*>(s.a[i] + off) = p[i];
 }
 
 // The two tensor-core stages of a tile whose stage-1 operands are in place
 // (see dft1024_tile); every thread of the block calls it.
-template <bool BF16, class Y, class M>
+template <class SP, class Y, class M>
 __device__ __forceinline__ bool dft1024_stages(const TileSmem& s, uint32_t& phase, int tid, Y y, M mid, float sc1,
                                                float sc2) {
   const int t = tid >> 5, lane = tid & 31;
   fence_async_smem();
   __syncthreads();
   mid();
-  if (tid == 0) issue_stage<BF16>(s);
+  if (tid == 0) issue_stage<SP>(s);
   bool ok = mbar_wait(s.bar, phase, kWaitLimit);
   phase ^= 1u;
   fence_after();
@@ -222,27 +223,27 @@ __device__ __forceinline__ bool dft1024_stages(const TileSmem& s, uint32_t& phas
 #pragma unroll
     for (int c = 0; c < 16; ++c) {
       const float2 z = scale2(cmul(make_float2(v[2 * c], v[2 * c + 1]), s.w[lane * c]), sc2);
-      uint32_t p[Parts<BF16>::n];
-      splitn<BF16>(z, p);
+      uint32_t p[SP::n];
+      splitn<SP>(z, p);
 #pragma unroll
-      for (int i = 0; i < Parts<BF16>::n; ++i)
+      for (int i = 0; i < SP::n; ++i)
         *reinterpret_cast<uint32_t*>(s.a[i] + kmaj_off(32 * t + c, 2 * lane)) = p[i];
     }
     tmem_ld32(lane_addr + 32, v);
 #pragma unroll
     for (int c = 0; c < 16; ++c) {
       const float2 z = scale2(cmul(make_float2(v[2 * c], v[2 * c + 1]), s.w[lane * (c + 16)]), sc2);
-      uint32_t p[Parts<BF16>::n];
-      splitn<BF16>(z, p);
+      uint32_t p[SP::n];
+      splitn<SP>(z, p);
 #pragma unroll
-      for (int i = 0; i < Parts<BF16>::n; ++i)
+      for (int i = 0; i < SP::n; ++i)
         *reinterpret_cast<uint32_t*>(s.a[i] + kmaj_off(32 * t + c + 16, 2 * lane)) = p[i];
     }
   }
   fence_before();
   fence_async_smem();
   __syncthreads();
-  if (tid == 0) issue_stage<BF16>(s);
+  if (tid == 0) issue_stage<SP>(s);
   ok = mbar_wait(s.bar, phase, kWaitLimit) && ok;
   phase ^= 1u;
   fence_after();
@@ -266,22 +267,22 @@ __device__ __forceinline__ bool dft1024_stages(const TileSmem& s, uint32_t& phas
 // the operands of the two stages by powers of two (the FP16 form keeps them
 // in range); the outputs are scaled back exactly.  Returns false if a
 // bounded wait on the tensor cores gave up.
-template <bool BF16, class X, class Y, class M>
+template <class SP, class X, class Y, class M>
 __device__ __forceinline__ bool dft1024_tile(const TileSmem& s, uint32_t& phase, int tid, X x, Y y, M mid,
                                              float sc1 = 1.f, float sc2 = 1.f) {
   const int t = tid >> 5, lane = tid & 31;
   // stage 1: row tid = (t, b = lane) holds x[32a + b], a = 0..31
-  constexpr int NP = Parts<BF16>::n;
+  constexpr int NP = SP::n;
 #pragma unroll
   for (int kc = 0; kc < 8; ++kc) {
     uint32_t p[4][NP];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) splitn<BF16>(scale2(x(t, 32 * (4 * kc + j) + lane), sc1), p[j]);
+    for (int j = 0; j < 4; ++j) splitn<SP>(scale2(x(t, 32 * (4 * kc + j) + lane), sc1), p[j]);
 #pragma unroll
     for (int i = 0; i < NP; ++i)
       *reinterpret_cast<uint4*>(s.a[i] + kmaj_off(tid, 8 * kc)) = make_uint4(p[0][i], p[1][i], p[2][i], p[3][i]);
   }
-  return dft1024_stages<BF16>(s, phase, tid, y, mid, sc1, sc2);
+  return dft1024_stages<SP>(s, phase, tid, y, mid, sc1, sc2);
 }
 
 // Copies the DFT-32 operand parts (kMaxParts logical [n][k] 64 x 64 16-bit
