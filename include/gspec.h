@@ -43,8 +43,9 @@ extern "C" {
 
 /* Arithmetic form of the FFT (gspec_config.form). */
 #define GSPEC_FORM_FP32 0 /* FP32 Stockham FFT on the CUDA cores */
-#define GSPEC_FORM_BF16 1 /* four-step DFT-32 stages on the tensor cores, BF16 hi+lo split, FP32 accumulate */
-#define GSPEC_FORM_FP16 2 /* the same with FP16 hi+lo halves */
+#define GSPEC_FORM_BF16 1 /* four-step DFT-32 stages on the tensor cores, operands split into BF16 parts
+                             (column pass: data 2 parts x matrix 3; row pass: 3 x 3), FP32 accumulate */
+#define GSPEC_FORM_FP16 2 /* the same with FP16 hi+lo halves (3 products) */
 
 /* Flags. */
 #define GSPEC_FLAG_SATURATION_RECORD 1u /* append n_out x {sat G0, sat G1} u64 to each output */
