@@ -294,6 +294,8 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
     f.njobs = h->d_njobs;
     f.dc = h->d_dc;
     f.dcsum = h->d_dcsum;
+    // each block holds whole outputs: the caller's zeroed bins take exactly one scatter
+    f.store_bins = h->n_blocks == 1 ? 1u : 0u;
     // job lists of every output spectrum of the block
     f.k0 = 0;
     f.nk = static_cast<uint32_t>(h->n_out);

@@ -115,7 +115,14 @@ __device__ __forceinline__ void fourstep_a_body(const FourStepParams& p) {
       if (SP <= BC || (e >= keep0 && e < keep0 + BC)) S[col * Cfg::STRIDE + spad(n1)] = make_float2(re[e], im[e]);
     }
   }
-  __syncthreads();
+  // dual pol: the gate statistics leave before the FFT, so they hold no
+  // registers there (single pol spills less with them committed at the end)
+  if constexpr (DUAL) {
+    commit_stats<NPOL>(p.c, st, k, 8 * static_cast<int>(N / 2 + 1), red, dc,
+                       p.dcsum + (static_cast<size_t>(k) * p.maxjobs + j) * 6);
+  } else {
+    __syncthreads();
+  }
   {
     const int sq = tid / Cfg::T1;
     const int t = tid - sq * Cfg::T1;
@@ -142,8 +149,9 @@ __device__ __forceinline__ void fourstep_a_body(const FourStepParams& p) {
       dst[static_cast<size_t>(k1) * N2 + n2] = cmul(v, W);
     }
   }
-  commit_stats<NPOL>(p.c, st, k, (DUAL ? 8 : 2) * static_cast<int>(N / 2 + 1), red, dc,
-                     p.dcsum + (static_cast<size_t>(k) * p.maxjobs + j) * 6);
+  if constexpr (!DUAL)
+    commit_stats<NPOL>(p.c, st, k, 2 * static_cast<int>(N / 2 + 1), red, dc,
+                       p.dcsum + (static_cast<size_t>(k) * p.maxjobs + j) * 6);
 }
 
 // Columns of up to 256 points (at most 256 threads) are held to 64 registers
@@ -346,38 +354,56 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, GSPEC_PASSB_MINB)
   }
 }
 
-// Adds the row-pair sums of one launch into the output spectra: thread per
-// output bin c (coalesced read-modify-write of the output record), reading
-// the slot a of row pair rp that holds c (the inverse of pair_slot):
-//   k1 = c % N1, k2 = c / N1; k1 = 0: rp 0, a = k2; k1 = N1/2: rp 0,
-//   a = N2/2 + 1 + k2; k1 < N1/2: rp = k1, a = k2; else rp = N1 - k1,
-//   a = N2/2 + k2.
-// grid = (ceil(C / 256), nk * VALS).
-__global__ void fourstep_scatter_kernel(FourStepParams p, int vals) {
+// Adds the row-pair sums of one launch into the output spectra.  Output bin
+// c = k1 + N1*k2 sits in row pair rp at slot a (the inverse of pair_slot):
+//   k1 = 0: rp 0, a = k2; k1 = N1/2: rp 0, a = N2/2 + 1 + k2;
+//   k1 < N1/2: rp = k1, a = k2; else rp = N1 - k1, a = N2/2 + k2.
+// Along k2 the slots are contiguous, along k1 the bins are, so a CTA moves a
+// 32 x 32 tile of (k1, k2) through shared memory: it reads 32 slots of each
+// of its 32 row pairs and writes 32 consecutive bins of each of its 32 k2
+// rows, both as 128-byte runs.  With store set (the launch holds every
+// contribution to its spectra, so the caller's zeroed bins would only be
+// read back) the bins are written instead of read, added and written.
+// grid = (N1 / 32, ceil((N2/2 + 1) / 32), nk * VALS), block = (32, 8).
+__global__ void __launch_bounds__(256) fourstep_scatter_kernel(FourStepParams p, int vals, int store) {
+  __shared__ float tile[32][33];
   const uint32_t N1 = p.N1, N2 = p.N2;
   const uint32_t C = N1 * N2 / 2 + 1;
-  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= C) return;
-  const uint32_t kk = blockIdx.y / vals;
-  const uint32_t v = blockIdx.y - kk * vals;
-  const uint32_t k1 = c % N1, k2 = c / N1;
-  uint32_t rp, a;
-  if (k1 == 0) {
-    rp = 0;
-    a = k2;
-  } else if (k1 == N1 / 2) {
-    rp = 0;
-    a = N2 / 2 + 1 + k2;
-  } else if (k1 < N1 / 2) {
-    rp = k1;
-    a = k2;
-  } else {
-    rp = N1 - k1;
-    a = N2 / 2 + k2;
+  const uint32_t kk = blockIdx.z / vals;
+  const uint32_t v = blockIdx.z - kk * vals;
+  const uint32_t k1_0 = blockIdx.x * 32, k2_0 = blockIdx.y * 32;
+  const uint32_t lane = threadIdx.x;
+  const size_t rp_stride = static_cast<size_t>(vals) * (N2 + 1);
+  const float* bs = p.bsum + (static_cast<size_t>(kk) * (N1 / 2) * vals + v) * (N2 + 1);
+#pragma unroll
+  for (uint32_t i = threadIdx.y; i < 32; i += 8) {
+    const uint32_t k1 = k1_0 + i, k2 = k2_0 + lane;
+    if (k1 + N1 * k2 >= C) continue;
+    uint32_t rp, a;
+    if (k1 == 0) {
+      rp = 0;
+      a = k2;
+    } else if (k1 == N1 / 2) {
+      rp = 0;
+      a = N2 / 2 + 1 + k2;
+    } else if (k1 < N1 / 2) {
+      rp = k1;
+      a = k2;
+    } else {
+      rp = N1 - k1;
+      a = N2 / 2 + k2;
+    }
+    tile[i][lane] = bs[rp * rp_stride + a];
   }
-  const float add = p.bsum[((static_cast<size_t>(kk) * (N1 / 2) + rp) * vals + v) * (N2 + 1) + a];
-  float* outf = reinterpret_cast<float*>(p.c.out + (p.k0 + kk) * p.c.out_rec);
-  outf[static_cast<size_t>(v) * C + c] += add;
+  __syncthreads();
+  float* outf = reinterpret_cast<float*>(p.c.out + (p.k0 + kk) * p.c.out_rec) + static_cast<size_t>(v) * C;
+#pragma unroll
+  for (uint32_t i = threadIdx.y; i < 32; i += 8) {
+    const uint32_t c = k1_0 + lane + N1 * (k2_0 + i);
+    if (c >= C) continue;
+    const float x = tile[lane][i];
+    outf[c] = store ? x : outf[c] + x;
+  }
 }
 
 // ------------------------------------------------------------ dispatch
@@ -467,8 +493,8 @@ cudaError_t launch_fourstep(int N, int nbits, bool dual, const FourStepParams& p
   }
   if (pass == 2) {
     const int vals = dual ? 8 : 2;
-    const uint32_t C = p.N1 * p.N2 / 2 + 1;
-    fourstep_scatter_kernel<<<dim3((C + 255) / 256, p.nk * vals), 256, 0, s>>>(p, vals);
+    fourstep_scatter_kernel<<<dim3(p.N1 / 32, (p.N2 / 2 + 1 + 31) / 32, p.nk * vals), dim3(32, 8), 0, s>>>(
+        p, vals, p.store_bins ? 1 : 0);
     return cudaGetLastError();
   }
   if (p.form != 0 && ((pass == 0 && p.N1 == 1024) || (pass == 1 && p.N2 == 1024)))
