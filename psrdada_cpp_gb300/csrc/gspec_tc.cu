@@ -165,7 +165,14 @@ namespace gspec {
 namespace tc {
 
 constexpr int kPassThreads = 128;
-constexpr int kColStride = spad_size(1024) + 1;   // odd: column-wise reads are conflict-free
+// Transformed columns of a pass-A tile (written over its operands): column t
+// at t * kColStride float2, tile 1's columns kTileSkew float2 further on.  The
+// store phase reads (8 columns) x (4 consecutive k1) per warp: with the stride
+// = 4 (mod 16) float2 and the skew the 16 lanes of each 8-byte wavefront hit
+// distinct banks.
+constexpr int kColStride = 1092;
+constexpr int kTileSkew = 2;
+static_assert(kColStride >= spad_size(1024) && kColStride % 16 == 4, "column stride");
 constexpr int kRowStride = spad_size(1024);
 
 // FP16 operand scales (powers of two): pass A inputs are at most 2^11 in
@@ -199,7 +206,7 @@ struct PassALayout {
   static constexpr size_t RED = B + kImageBytes;
   static constexpr size_t BAR = RED + (THREADS / 32) * 12 * 8;
   static constexpr size_t BYTES = BAR + 32;
-  static_assert(static_cast<size_t>(4) * kColStride * sizeof(float2) <= TILE, "columns fit the operands");
+  static_assert(static_cast<size_t>(4 * kColStride + kTileSkew) * sizeof(float2) <= TILE, "columns fit the operands");
 };
 
 // grid.x = nk * maxjobs * (N2 / 8): (output spectrum, job, 8 columns).  The
@@ -274,7 +281,11 @@ __global__ void __launch_bounds__(PassALayout<BF16>::THREADS, SplitA<BF16>::n ==
                 "per-thread gate statistics fit the 32-bit commit");
   GateStats st[NPOL];
   DcAcc dc[2];
-  for (int n1 = tid; n1 < N1; n1 += THREADS) {
+  // row n1 = 32 a + b goes to operand row b, K pair a (put_stage1): lanes
+  // take consecutive a, so that their operand stores hit distinct banks
+  static_assert(THREADS == 256 && N1 == 1024, "lanes a = 0..31, b = warp + 8 i");
+  for (int i = 0; i < 4; ++i) {
+    const int n1 = 32 * (tid & 31) + (tid >> 5) + 8 * i;
     const uint32_t off = N2 * n1 + gbase;
     float re[SP], im[SP];
     if constexpr (DUAL) {
@@ -302,7 +313,7 @@ __global__ void __launch_bounds__(PassALayout<BF16>::THREADS, SplitA<BF16>::n ==
   fence_after();
   s.tmem = *tmem_slot + grp * kTmemCols;
   uint32_t phase = 0;
-  float2* S = reinterpret_cast<float2*>(s.a[0]);          // this tile's columns after the transform
+  float2* S = reinterpret_cast<float2*>(s.a[0]) + grp * kTileSkew;   // this tile's columns after the transform
   const bool ok = dft1024_stages<SplitA<BF16>>(
       s, phase, gtid, [&](int t, int k1, float2 v) { S[t * kColStride + spad(k1)] = v; }, [] {}, sc1, sc2);
   if (!ok && gtid == 0 && p.c.dev_err) atomicExch(p.c.dev_err, 3u);
@@ -314,7 +325,8 @@ __global__ void __launch_bounds__(PassALayout<BF16>::THREADS, SplitA<BF16>::n ==
     constexpr int PPT = N1 / KS;
     const int col = tid % BC;
     const uint32_t n2 = c0 + col;
-    const float2* Sc = reinterpret_cast<const float2*>(smem + L::A + (col >> 2) * L::TILE) + (col & 3) * kColStride;
+    const float2* Sc = reinterpret_cast<const float2*>(smem + L::A + (col >> 2) * L::TILE) + (col >> 2) * kTileSkew +
+                       (col & 3) * kColStride;
     auto exact = [&](uint32_t m) { return cmul(__ldg(&p.twA[m >> 10]), __ldg(&p.twB[m & 1023])); };
     const float2 D = exact(n2 * KS);
     float2 W = make_float2(1.f, 0.f);
