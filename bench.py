@@ -359,7 +359,9 @@ def cpu_chain_rate(spec, kind: str, seconds: float = 10.0, max_blocks: int = 1 <
 
 
 # ---------------------------------------------------------------- GPU arm
-FORM_DTYPE = {"fp32": "f32", "bf16": "bf16 hi+lo, f32 accumulate", "fp16": "f16 hi+lo, f32 accumulate"}
+FORM_DTYPE = {"fp32": "f32",
+              "bf16": "bf16 split operands (column pass 2x3 parts, row pass 3x3), f32 accumulate",
+              "fp16": "f16 hi+lo operands, f32 accumulate"}
 
 
 def stokes_rel_err(got: np.ndarray, ref: np.ndarray, dual: bool, floor: float = 1e-2):
@@ -877,8 +879,8 @@ def main(argv=None):
                     help="c1-c3 one stream (c2m: c2 with a 61-heap diode period); c4 16 uneven streams in one "
                          "CUDA graph; c5 the serving loop")
     ap.add_argument("--form", choices=["fp32", "bf16", "fp16"], default=None,
-                    help="FFT arithmetic: FP32 CUDA cores, or tensor-core DFT-32 stages with BF16/FP16 hi+lo "
-                         "halves (default: bf16 for c3, fp32 otherwise)")
+                    help="FFT arithmetic: FP32 CUDA cores, or tensor-core DFT-32 stages with split BF16/FP16 "
+                         "operands (default: bf16 for c3, fp32 otherwise)")
     ap.add_argument("--no-compare", action="store_true",
                     help="time only --form (by default a tensor-core form is timed beside the FP32 form)")
     ap.add_argument("--no-e2e", action="store_true")

@@ -215,14 +215,6 @@ cudaError_t timed(gspec_handle* h, int kind, cudaStream_t s, F&& launch) {
   return e;
 }
 
-// Copies the device error word to its pinned host mirror behind the block's
-// kernels (no copy when the caller supplied no mirror).
-cudaError_t refresh_error_word(gspec_handle* h, cudaStream_t s) {
-  if (!h->h_err_dev || !h->d_err) return cudaSuccess;
-  ++h->launches;
-  return launch_mirror_word(h->d_err, h->h_err_dev, s);
-}
-
 // Error status of the kernels that completed so far.
 int device_error(gspec_handle* h) {
   if (h->h_err && *h->h_err) {
@@ -249,6 +241,7 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
   p.frames_per_unit = h->frames_per_unit;
   p.flags = h->d_flags;
   p.dev_err = h->d_err;
+  p.err_host = h->d_err ? h->h_err_dev : nullptr;   // refreshed by the block's finalisation
   const int N = static_cast<int>(h->cfg.fft_length);
   cudaError_t e;
   // gate masks per item and the gates each frame holds data in
@@ -268,13 +261,10 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
     if (e != cudaSuccess) return e;
     if (h->slices > 1) {
       // partial spectra of the slices, then the baselines of the next block
-      e = timed(h, 1, s, [&] {
-        return launch_reduce_finalize(N, h->dual, p, h->npol, static_cast<int>(h->cfg.convention), h->d_baselines,
-                                      s);
+      return timed(h, 1, s, [&] {
+        return launch_reduce_finalize(N, h->dual, p, h->npol, static_cast<int>(h->cfg.convention),
+                                      h->ungated ? 1 : 0, h->d_baselines, s);
       });
-      if (e != cudaSuccess) return e;
-      if (h->ungated && (e = cudaMemsetAsync(h->d_baselines, 0, 4 * sizeof(float), s)) != cudaSuccess) return e;
-      return refresh_error_word(h, s);
     }
   } else {
     FourStepParams f{};
@@ -316,14 +306,10 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
       if (e != cudaSuccess) return e;
     }
   }
-  e = timed(h, 4, s, [&] {
+  return timed(h, 4, s, [&] {
     return launch_finalize(p, h->npol, static_cast<int>(h->C), h->dual ? 1 : 0, static_cast<int>(h->cfg.convention),
-                           h->d_baselines, s);
+                           h->ungated ? 1 : 0, h->d_baselines, s);
   });
-  if (e != cudaSuccess) return e;
-  // no gate, no baseline: the samples enter the FFT as they are ((v - 0) + 0 = v)
-  if (h->ungated && (e = cudaMemsetAsync(h->d_baselines, 0, 4 * sizeof(float), s)) != cudaSuccess) return e;
-  return refresh_error_word(h, s);
 }
 
 uint64_t env_u64(const char* name, uint64_t dflt) {

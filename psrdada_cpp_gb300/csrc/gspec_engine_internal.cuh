@@ -59,7 +59,7 @@ struct gspec_handle {
   int32_t heap_shift = -1;
   uint32_t* d_err = nullptr;       // set by kernels whose bounded waits gave up
   uint32_t* h_err = nullptr;       // pinned copy, refreshed after every block
-  uint32_t* h_err_dev = nullptr;   // its device address (written by mirror_word_kernel)
+  uint32_t* h_err_dev = nullptr;   // its device address (written by the block's finalisation)
   cudaStream_t h2d = nullptr, proc = nullptr, d2h = nullptr;
   cudaEvent_t ev_h2d[2] = {}, ev_in_free[2] = {}, ev_out_ready[2] = {};
   int ia = 1, oa = 0, ha = 0, handed = -1;

@@ -308,13 +308,17 @@ __global__ void gate_prepass_kernel(GateParams g, uint32_t nitems, uint8_t* mask
 
 // Baselines for the next block (edd/src/GatedSpectrometer.cu:98-118), with
 // exact integer sums, an FP64 division and a zero-count guard; then the
-// Stokes record's counter copies (edd/src/GatedSpectrometer.cu:485-525).
-// Run by one warp after every counter of the block is final.
-__device__ void finalize_warp(const ChainParams& p, int npol, int C, int dual, int convention, float* baselines_out) {
-  const int lane = threadIdx.x & 31;
+// Stokes record's counter copies (edd/src/GatedSpectrometer.cu:485-525),
+// and the device error word into its page-locked host mirror.  Run by every
+// thread of one CTA after every counter of the block is final.
+__device__ void finalize_block(const ChainParams& p, int npol, int C, int dual, int convention, int ungated,
+                               float* baselines_out) {
+  __shared__ unsigned long long red[2 * 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = (blockDim.x + 31) >> 5;
   const int vals = dual ? 8 : 2;
   unsigned long long t0 = 0, t1 = 0;
-  for (uint32_t k = lane; k < p.n_out; k += 32) {
+  for (uint32_t k = threadIdx.x; k < p.n_out; k += blockDim.x) {
     const unsigned long long* cnt =
         reinterpret_cast<const unsigned long long*>(p.out + k * p.out_rec + static_cast<uint64_t>(vals) * C * 4);
     t0 += cnt[0];
@@ -323,6 +327,16 @@ __device__ void finalize_warp(const ChainParams& p, int npol, int C, int dual, i
   t0 = warp_sum_u64(t0);
   t1 = warp_sum_u64(t1);
   if (lane == 0) {
+    red[2 * warp] = t0;
+    red[2 * warp + 1] = t1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    t0 = t1 = 0;
+    for (int w = 0; w < nwarps; ++w) {
+      t0 += red[2 * w];
+      t1 += red[2 * w + 1];
+    }
     for (int pol = 0; pol < npol; ++pol) {
       unsigned long long* ps = p.pol_stats + pol * kPolStats;
       unsigned long long den0 = ps[0], den1 = ps[1];
@@ -337,31 +351,38 @@ __device__ void finalize_warp(const ChainParams& p, int npol, int C, int dual, i
       }
       const long long s0 = static_cast<long long>(ps[2]);
       const long long s1 = static_cast<long long>(ps[3]);
-      baselines_out[2 * pol + 0] = den0 ? static_cast<float>(static_cast<double>(s0) / static_cast<double>(den0)) : 0.f;
-      baselines_out[2 * pol + 1] = den1 ? static_cast<float>(static_cast<double>(s1) / static_cast<double>(den1)) : 0.f;
+      // ungated: no gate, no baseline ((v - 0) + 0 = v for the next block)
+      baselines_out[2 * pol + 0] =
+          (den0 && !ungated) ? static_cast<float>(static_cast<double>(s0) / static_cast<double>(den0)) : 0.f;
+      baselines_out[2 * pol + 1] =
+          (den1 && !ungated) ? static_cast<float>(static_cast<double>(s1) / static_cast<double>(den1)) : 0.f;
     }
     for (int i = 0; i < npol * kPolStats; ++i) p.pol_stats[i] = 0;
+    // the error word of the block's kernels (all of them ran before this one)
+    if (p.err_host) *p.err_host = *p.dev_err;
   }
   if (dual) {
-    for (uint32_t k = lane; k < p.n_out; k += 32) {
+    for (uint32_t k = threadIdx.x; k < p.n_out; k += blockDim.x) {
       unsigned long long* cnt =
           reinterpret_cast<unsigned long long*>(p.out + k * p.out_rec + static_cast<uint64_t>(vals) * C * 4);
+      const unsigned long long c0 = cnt[0], c1 = cnt[1];
       for (int r = 1; r < 4; ++r) {
-        cnt[2 * r] = cnt[0];
-        cnt[2 * r + 1] = cnt[1];
+        cnt[2 * r] = c0;
+        cnt[2 * r + 1] = c1;
       }
     }
   }
 }
 
-__global__ void finalize_kernel(ChainParams p, int npol, int C, int dual, int convention, float* baselines_out) {
-  finalize_warp(p, npol, C, dual, convention, baselines_out);
+__global__ void finalize_kernel(ChainParams p, int npol, int C, int dual, int convention, int ungated,
+                                float* baselines_out) {
+  finalize_block(p, npol, C, dual, convention, ungated, baselines_out);
 }
 
 // out[k][i] += sum_s partial[k][s][i] (fixed order); the last block of the
 // grid also runs the block finalisation (the counters are final already).
 __global__ void reduce_finalize_kernel(ChainParams p, int vals_c, int npol, int C, int dual, int convention,
-                                       float* baselines_out) {
+                                       int ungated, float* baselines_out) {
   const uint32_t k = blockIdx.y;
   float* outf = reinterpret_cast<float*>(p.out + k * p.out_rec);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < vals_c; i += gridDim.x * blockDim.x) {
@@ -370,8 +391,8 @@ __global__ void reduce_finalize_kernel(ChainParams p, int vals_c, int npol, int 
     for (uint32_t s = 0; s < p.slices; ++s) v += src[static_cast<size_t>(s) * vals_c];
     outf[i] += v;
   }
-  if (blockIdx.x == gridDim.x - 1 && blockIdx.y == gridDim.y - 1 && threadIdx.x < 32)
-    finalize_warp(p, npol, C, dual, convention, baselines_out);
+  if (blockIdx.x == gridDim.x - 1 && blockIdx.y == gridDim.y - 1)
+    finalize_block(p, npol, C, dual, convention, ungated, baselines_out);
 }
 
 // --------------------------------------------------------------- twiddles
@@ -504,12 +525,12 @@ cudaError_t launch_small_chain(int N, int nbits, bool dual, const ChainParams& p
   return dual ? launch_small_d<true>(N, nbits, p, s) : launch_small_d<false>(N, nbits, p, s);
 }
 
-cudaError_t launch_reduce_finalize(int N, bool dual, const ChainParams& p, int npol, int convention,
+cudaError_t launch_reduce_finalize(int N, bool dual, const ChainParams& p, int npol, int convention, int ungated,
                                    float* baselines_out, cudaStream_t s) {
   const int C = N / 2 + 1;
   const int vals_c = (dual ? 8 : 2) * C;
   dim3 grid((vals_c + 255) / 256, p.n_out);
-  reduce_finalize_kernel<<<grid, 256, 0, s>>>(p, vals_c, npol, C, dual ? 1 : 0, convention, baselines_out);
+  reduce_finalize_kernel<<<grid, 256, 0, s>>>(p, vals_c, npol, C, dual ? 1 : 0, convention, ungated, baselines_out);
   return cudaGetLastError();
 }
 
@@ -521,9 +542,9 @@ cudaError_t launch_prepass(const GateParams& g, uint32_t nitems, uint8_t* masks,
   return cudaGetLastError();
 }
 
-cudaError_t launch_finalize(const ChainParams& p, int npol, int C, int dual, int convention, float* baselines_out,
-                            cudaStream_t s) {
-  finalize_kernel<<<1, 32, 0, s>>>(p, npol, C, dual, convention, baselines_out);
+cudaError_t launch_finalize(const ChainParams& p, int npol, int C, int dual, int convention, int ungated,
+                            float* baselines_out, cudaStream_t s) {
+  finalize_kernel<<<1, 256, 0, s>>>(p, npol, C, dual, convention, ungated, baselines_out);
   return cudaGetLastError();
 }
 
@@ -571,12 +592,6 @@ cudaError_t launch_unpack(int nbits, const uint8_t* raw, uint64_t nsamples, floa
 // Mirrors the device error word into host memory (page-locked, device
 // accessible) with one store from an SM: no copy engine is involved, so the
 // status of a block never waits behind other streams' bulk copies.
-__global__ void mirror_word_kernel(const uint32_t* __restrict__ src, volatile uint32_t* dst) { *dst = *src; }
-
-cudaError_t launch_mirror_word(const uint32_t* src, uint32_t* dst, cudaStream_t s) {
-  mirror_word_kernel<<<1, 1, 0, s>>>(src, dst);
-  return cudaGetLastError();
-}
 
 // Copies between device memory and page-locked host memory with SM loads and
 // stores (small blocks of the serving loop, which then never queue behind

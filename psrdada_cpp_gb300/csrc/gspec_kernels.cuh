@@ -29,6 +29,7 @@ struct ChainParams {
   uint32_t slices;                 // work units per output spectrum
   uint32_t frames_per_unit;
   uint32_t* dev_err;               // set non-zero when a bounded device wait gives up
+  volatile uint32_t* err_host;     // page-locked mirror of *dev_err written by the finalisation (or null)
 };
 
 // Large-N (four-step) parameters.
@@ -56,17 +57,16 @@ struct FourStepParams {
 
 // Host-side launchers (gspec_kernels.cu).
 cudaError_t launch_small_chain(int N, int nbits, bool dual, const ChainParams& p, cudaStream_t s);
-cudaError_t launch_reduce_finalize(int N, bool dual, const ChainParams& p, int npol, int convention,
+cudaError_t launch_reduce_finalize(int N, bool dual, const ChainParams& p, int npol, int convention, int ungated,
                                    float* baselines_out, cudaStream_t s);
-cudaError_t launch_finalize(const ChainParams& p, int npol, int C, int dual, int convention, float* baselines_out,
-                            cudaStream_t s);
+cudaError_t launch_finalize(const ChainParams& p, int npol, int C, int dual, int convention, int ungated,
+                            float* baselines_out, cudaStream_t s);
 cudaError_t launch_twiddles(int N, float2* tw, cudaStream_t s);
 cudaError_t launch_fourstep_twiddles(int N, float2* twA, float2* twB, cudaStream_t s);
 cudaError_t launch_gate_debug(int nbits, const GateParams& g, const float* baselines, int npol, uint32_t nsamps,
                               float* out, cudaStream_t s);
 cudaError_t launch_unpack(int nbits, const uint8_t* raw, uint64_t nsamples, float* out, cudaStream_t s);
 // One store of *src into device-accessible host memory dst.
-cudaError_t launch_mirror_word(const uint32_t* src, uint32_t* dst, cudaStream_t s);
 // bytes (a multiple of 8) from device memory to device-accessible host memory by SM stores.
 cudaError_t launch_copy_words(void* dst, const void* src, uint64_t bytes, int sm_count, cudaStream_t s);
 cudaError_t launch_fourstep(int N, int nbits, bool dual, const FourStepParams& p, int pass, cudaStream_t s);
