@@ -61,19 +61,28 @@ L2_FALLBACK = 129 * 2**20                            # GB300 L2 size when the de
 
 
 # ------------------------------------------------------------------ helpers
-def workload(name: str):
+def workload(name: str, frames: int = 0):
+    """(stream spec, sample kind) of a one-stream workload; frames > 0 shrinks its block
+    to that many fft frames per pol (same kernels and launch shapes per chunk: for
+    small ncu captures, never for a bench line)."""
     import dataclasses
     from psrdada_cpp_gb300 import synth
     if name == "c1":
-        return synth.config1(), "c1"
-    if name == "c3":
-        return synth.config3(), "c3"
-    if name == "c2m":
+        spec, kind = synth.config1(), "c1"
+    elif name == "c3":
+        spec, kind = synth.config3(), "c3"
+    elif name == "c2m":
         # the diode period (61 heaps of 4096 samples) is not a whole number of 2^16-sample frames:
         # frames straddling a toggle hold data in both gates, the others in one
         c2 = synth.config2()
-        return dataclasses.replace(c2, name=c2.name + "_diode61", diode_period_heaps=61), "c2"
-    return synth.config2(), "c2"
+        spec, kind = dataclasses.replace(c2, name=c2.name + "_diode61", diode_period_heaps=61), "c2"
+    else:
+        spec, kind = synth.config2(), "c2"
+    if frames > 0:
+        if frames % spec.naccumulate:
+            raise SystemExit(f"--frames must be a multiple of naccumulate ({spec.naccumulate})")
+        spec = dataclasses.replace(spec, name=f"{spec.name}_frames{frames}", samples_per_pol=frames * spec.fft_length)
+    return spec, kind
 
 
 def dist_env():
@@ -542,7 +551,7 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
     from psrdada_cpp_gb300 import synth
 
-    spec, kind = workload(args.workload)
+    spec, kind = workload(args.workload, args.frames)
     forms = [args.form] + ([] if args.form == "fp32" or args.no_compare else ["fp32"])
     # two host blocks where they are cheap to make; one (used twice) at 2^28 samples/pol
     nhost = 1 if spec.samples_per_pol >= (1 << 27) else 2
@@ -884,6 +893,9 @@ def main(argv=None):
     ap.add_argument("--no-compare", action="store_true",
                     help="time only --form (by default a tensor-core form is timed beside the FP32 form)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--frames", type=int, default=0,
+                    help="c1-c3: shrink the block to this many fft frames per pol (small cases for ncu captures; "
+                         "its lines are not the workload's bench line)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="wall seconds of the timed CPU sample")
     ap.add_argument("--ref-budget-s", type=float, default=150.0)

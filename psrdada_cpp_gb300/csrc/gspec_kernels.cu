@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS, GSPEC_SMALL_MINB)
 // item_index(first) .. item_index(last) in steps of nsc (the index is
 // monotonic inside a gating chunk and frames never straddle chunks).
 __global__ void gate_prepass_kernel(GateParams g, uint32_t nitems, uint8_t* masks, uint32_t N, uint32_t nframes,
-                                    uint8_t* flags) {
+                                    uint8_t* flags, uint32_t L) {
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nitems; i += stride) {
     bool m0, m1;
@@ -294,15 +294,25 @@ __global__ void gate_prepass_kernel(GateParams g, uint32_t nitems, uint8_t* mask
     masks[i] = static_cast<uint8_t>(m0 | (m1 << 1));
   }
   if (!flags) return;
-  for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < nframes; f += stride) {
-    const uint32_t i0 = item_index(g, f * N), i1 = item_index(g, f * N + N - 1);
+  // L lanes per frame (a power of two up to 32, about the items a frame
+  // spans: 256 at 2^20 samples and 4096-sample heaps, 1 at 1024 samples);
+  // the warp loop is uniform so that every lane takes part in the shuffles
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t fpw = 32 / L;
+  const uint32_t f_sub = lane / L, sub = lane & (L - 1);
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * fpw < nframes; w += stride >> 5) {
+    const uint32_t f = w * fpw + f_sub;
     uint32_t fl = 0;
-    for (uint32_t i = i0; i <= i1; i += g.nsc) {
-      bool m0, m1;
-      item_masks(load_item(g, i), g.bitpos, m0, m1);
-      fl |= m0 | (m1 << 1);
+    if (f < nframes) {
+      const uint32_t i0 = item_index(g, f * N), i1 = item_index(g, f * N + N - 1);
+      for (uint32_t i = i0 + sub * g.nsc; i <= i1; i += L * g.nsc) {
+        bool m0, m1;
+        item_masks(load_item(g, i), g.bitpos, m0, m1);
+        fl |= m0 | (m1 << 1);
+      }
     }
-    flags[f] = static_cast<uint8_t>(fl);
+    for (uint32_t o = L / 2; o > 0; o >>= 1) fl |= __shfl_xor_sync(0xffffffffu, fl, o);
+    if (f < nframes && sub == 0) flags[f] = static_cast<uint8_t>(fl);
   }
 }
 
@@ -536,9 +546,13 @@ cudaError_t launch_reduce_finalize(int N, bool dual, const ChainParams& p, int n
 
 cudaError_t launch_prepass(const GateParams& g, uint32_t nitems, uint8_t* masks, uint32_t N, uint32_t nframes,
                            uint8_t* flags, cudaStream_t s) {
-  const uint32_t work = std::max(nitems, nframes);
-  const unsigned grid = std::min<unsigned>(4 * 152, (work + 255) / 256);
-  gate_prepass_kernel<<<grid ? grid : 1, 256, 0, s>>>(g, nitems, masks, N, nframes, flags);
+  // lanes per frame: the items a frame spans, as a power of two up to 32
+  const uint64_t span = (static_cast<uint64_t>(N) * g.nbits / 8 + g.heap_size - 1) / std::max<uint64_t>(g.heap_size, 1);
+  uint32_t L = 1;
+  while (L < 32 && L < span) L <<= 1;
+  const uint64_t work = std::max<uint64_t>(nitems, static_cast<uint64_t>(nframes) * L);
+  const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(4 * 152, (work + 255) / 256));
+  gate_prepass_kernel<<<grid ? grid : 1, 256, 0, s>>>(g, nitems, masks, N, nframes, flags, L);
   return cudaGetLastError();
 }
 
