@@ -147,14 +147,33 @@ __host__ __device__ constexpr int tw_offset(int n, int ns) {
 }
 __host__ __device__ constexpr int tw_size(int n) { return tw_offset(n, n); }
 
+// Barrier of a group of threads that share data: the whole CTA
+// (kSyncCta), the calling warp (kSyncWarp: the group lies within one warp,
+// every thread of the warp calls it) or the named barrier `id` of `count`
+// threads (kSyncNamed: whole warps, ids 1..15; id 0 is __syncthreads').
+constexpr int kSyncCta = 0, kSyncWarp = 1, kSyncNamed = 2;
+template <int SYNC>
+__device__ __forceinline__ void group_sync(int id, int count) {
+  if constexpr (SYNC == kSyncWarp) {
+    __syncwarp();
+  } else if constexpr (SYNC == kSyncNamed) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+  } else {
+    __syncthreads();
+  }
+}
+
 // One in-place FFT of N points in padded shared memory S, done by the
 // T = N/P threads with index t of the calling group.  Every thread of the
-// block must call it the same number of times (it contains __syncthreads).
+// group's barrier (group_sync<SYNC>: the CTA by default) must call it the
+// same number of times.
 // tw: per-pass tables, entry [k][q] = exp(-2 pi i q k / (ns R)) at
 // tw_offset(N, ns) + k*ns + q; the kernels keep a copy in shared memory
 // (load_twiddles) so the passes do not wait on global loads.
-template <int N, int P, int NS = 1>
-__device__ __forceinline__ void fft_smem(float2* S, const float2* tw, int t, bool active) {
+template <int N, int P, int NS = 1, int SYNC = kSyncCta>
+__device__ __forceinline__ void fft_smem(float2* S, const float2* tw, int t, bool active, int bar_id = 0) {
+  static_assert(SYNC != kSyncWarp || N / P <= 32, "a warp-synchronous FFT lies within one warp");
+  auto sync = [&] { group_sync<SYNC>(bar_id, N / P); };
   if constexpr (NS < N) {
     constexpr int R = pass_radix(N, NS);
     constexpr int T = N / P;
@@ -169,7 +188,7 @@ __device__ __forceinline__ void fft_smem(float2* S, const float2* tw, int t, boo
         for (int k = 0; k < R; ++k) v[u][k] = S[spad(j + k * (N / R))];
       }
     }
-    __syncthreads();
+    sync();
     if (active) {
 #pragma unroll
       for (int u = 0; u < NB; ++u) {
@@ -186,8 +205,8 @@ __device__ __forceinline__ void fft_smem(float2* S, const float2* tw, int t, boo
         for (int k = 0; k < R; ++k) S[spad(base + k * NS)] = v[u][k];
       }
     }
-    __syncthreads();
-    fft_smem<N, P, NS * R>(S, tw, t, active);
+    sync();
+    fft_smem<N, P, NS * R, SYNC>(S, tw, t, active, bar_id);
   }
 }
 

@@ -105,6 +105,11 @@ struct SmallCfg {
   static constexpr int T = N / P;                 // threads per FFT
   static constexpr int NSLOT = T >= 256 ? 1 : 256 / T;
   static constexpr int THREADS = NSLOT * T;
+  // a slot's sequence and accumulator are touched by its own threads only,
+  // so a round needs the slot's barrier only: its warp (T <= 32) or a named
+  // barrier of its T threads (id 1 + slot), the CTA when one slot fills it
+  static constexpr int SYNC = T <= 32 ? kSyncWarp : (NSLOT > 1 ? kSyncNamed : kSyncCta);
+  static_assert(SYNC != kSyncNamed || NSLOT <= 15, "named barrier ids 1..15");
   static constexpr int C = N / 2 + 1;
   static constexpr int VALS = DUAL ? 8 : 2;
   static constexpr int SEQ_F2 = spad_size(N);
@@ -174,6 +179,7 @@ __global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS, GSPEC_SMALL_MINB)
   GateStats st[NPOL];
   float2* Z = S + slot * Cfg::SEQ_F2;
   float* A = acc + slot * Cfg::VALS * C;
+  auto round_sync = [&] { group_sync<Cfg::SYNC>(1 + slot, Cfg::T); };
 
   for (uint32_t it = 0; it < njobs; it += Cfg::NSLOT) {
     const uint32_t jx = it + slot;
@@ -181,25 +187,30 @@ __global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS, GSPEC_SMALL_MINB)
     const uint32_t job = active ? jobs[jx] : 0u;
     const uint32_t fa = job_fa(job), ga = job_ga(job), fb = job_fb(job), gb = job_gb(job);
     if (active) {
+      // spans of SP samples: whole 32-bit words from a group start (8 samples
+      // at 8 and 12 bits, 16 at 10 bits), so a thread holds fewer values than
+      // a whole 16- or 32-sample group would take
+      constexpr int SP = NBITS == 10 ? 16 : 8;
+      static_assert(G % SP == 0 && (SP * NBITS) % 32 == 0, "spans are whole words within a group");
 #pragma unroll 1
-      for (int gi = t; gi < NG; gi += Cfg::T) {
-        const uint32_t sa = (f0 + fa) * N + gi * G;
-        float re[G], im[G];
+      for (int gi = t; gi < N / SP; gi += Cfg::T) {
+        const uint32_t sa = (f0 + fa) * N + gi * SP;
+        float re[SP], im[SP];
         if constexpr (DUAL) {
-          gate_group_dual<NBITS>(p.g, sa, bl[ga], bl[2 + ga], ga, re, im, st[0], st[NPOL - 1], true);
+          gate_group_dual<NBITS, SP>(p.g, sa, bl[ga], bl[2 + ga], ga, re, im, st[0], st[NPOL - 1], true);
         } else if (fb == fa) {
-          gate_group<NBITS>(p.g, 0, sa, bl[0], bl[1], re, im, st[0], 3u);
+          gate_group<NBITS, SP>(p.g, 0, sa, bl[0], bl[1], re, im, st[0], 3u);
         } else {
-          gate_group1<NBITS>(p.g, 0, sa, bl[ga], ga, re, st[0], true);
+          gate_group1<NBITS, SP>(p.g, 0, sa, bl[ga], ga, re, st[0], true);
           if (fb != kNoFrame) {
-            gate_group1<NBITS>(p.g, 0, (f0 + fb) * N + gi * G, bl[gb], gb, im, st[0], true);
+            gate_group1<NBITS, SP>(p.g, 0, (f0 + fb) * N + gi * SP, bl[gb], gb, im, st[0], true);
           } else {
 #pragma unroll
-            for (int e = 0; e < G; ++e) im[e] = 0.f;
+            for (int e = 0; e < SP; ++e) im[e] = 0.f;
           }
         }
 #pragma unroll
-        for (int e = 0; e < G; ++e) Z[spad(gi * G + e)] = make_float2(re[e], im[e]);
+        for (int e = 0; e < SP; ++e) Z[spad(gi * SP + e)] = make_float2(re[e], im[e]);
       }
     }
     {
@@ -220,8 +231,8 @@ __global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS, GSPEC_SMALL_MINB)
         }
       }
     }
-    __syncthreads();
-    fft_smem<N, Cfg::P>(Z, twp, t, active);
+    round_sync();
+    fft_smem<N, Cfg::P, 1, Cfg::SYNC>(Z, twp, t, active, 1 + slot);
     if (active) {
 #pragma unroll 1
       for (int c = t; c < C; c += Cfg::T) {
@@ -244,8 +255,9 @@ __global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS, GSPEC_SMALL_MINB)
         }
       }
     }
-    __syncthreads();
+    round_sync();
   }
+  __syncthreads();
   // gates without data in a frame: constant baseline, bin 0 only
   if (tid == 0) {
     const float n = static_cast<float>(N);
