@@ -5,6 +5,8 @@
 # in oracle/ref_shim/ standing in for googletest, Boost.Log and psrdada.
 # The library exports the reference's host-side C reference functions
 # (see oracle/ref_shim/ref_exports.cu); it is used only to pin the oracle.
+# oracle/_ref/ref_kernels.cubin holds the reference's GPU kernels
+# (oracle/ref_shim/ref_kernels.cu) for the GPU pin test.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
 REF="${1:-${PSRDADA_CPP_TREE:-}}"
@@ -30,3 +32,9 @@ done
 for p in "${pids[@]}"; do wait "$p"; done
 "$NVCC" -gencode arch=compute_103a,code=sm_103a -shared -o "$OUT/libref_host.so" "${OBJS[@]}" -lcudart
 echo "built $OUT/libref_host.so"
+# the reference's GPU kernels as one module for the driver API (the GPU pin
+# test), with the kernels' symbol names as ptxas lists them
+"$NVCC" "${FLAGS[@]}" -Xptxas -v -cubin -x cu "$HERE/ref_shim/ref_kernels.cu" -o "$OUT/ref_kernels.cubin" \
+    2> "$OUT/ref_kernels.ptxas.txt"
+sed -n "s/.*Compiling entry function '\([^']*\)'.*/\1/p" "$OUT/ref_kernels.ptxas.txt" | sort -u > "$OUT/ref_kernels.names"
+echo "built $OUT/ref_kernels.cubin ($(wc -l < "$OUT/ref_kernels.names") kernels)"
