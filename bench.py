@@ -161,6 +161,35 @@ def ncu_traffic(kernel: str, workload_name: str):
     return None
 
 
+def bind_to_gpu_cpus(index: int, pci_bus_id: str | None = None):
+    """Binds this process to the host CPUs NVML reports as local to the GPU
+    (nvmlDeviceGetCpuAffinity, a read-only query), so that the page-locked
+    blocks and outputs it writes first land on the GPU's NUMA node.  Returns
+    the CPU list, or None where NVML or the call is unavailable."""
+    import ctypes
+    try:
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            return None
+        h = ctypes.c_void_p()
+        ok = bool(pci_bus_id) and lib.nvmlDeviceGetHandleByPciBusId_v2(pci_bus_id.encode(), ctypes.byref(h)) == 0
+        if not ok and lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(index), ctypes.byref(h)) != 0:
+            return None
+        words = 64
+        mask = (ctypes.c_ulong * words)()
+        if lib.nvmlDeviceGetCpuAffinity(h, ctypes.c_uint(words), mask) != 0:
+            return None
+        bits = ctypes.sizeof(ctypes.c_ulong) * 8
+        cpus = {w * bits + b for w in range(words) for b in range(bits) if (mask[w] >> b) & 1}
+        cpus &= os.sched_getaffinity(0)
+        if not cpus:
+            return None
+        os.sched_setaffinity(0, cpus)
+        return sorted(cpus)
+    except (OSError, AttributeError, ValueError):
+        return None
+
+
 class ClockSampler:
     """SM clock, power and clock-event (throttle) reasons sampled while the
     GPU works: read-only NVML queries through ctypes every 20 ms on a host
@@ -553,6 +582,9 @@ def run_gpu(args):
 
     spec, kind = workload(args.workload, args.frames)
     forms = [args.form] + ([] if args.form == "fp32" or args.no_compare else ["fp32"])
+    # host buffers on the GPU's NUMA node: run on the CPUs local to the GPU before any are written
+    all_cpus = os.sched_getaffinity(0)
+    host_cpus = bind_to_gpu_cpus(local, pci_bus_id(dev))
     # two host blocks where they are cheap to make; one (used twice) at 2^28 samples/pol
     nhost = 1 if spec.samples_per_pol >= (1 << 27) else 2
     host_blocks = [synth.make_block(spec, seed=1 + rank, block_index=i, kind=kind) for i in range(nhost)]
@@ -571,6 +603,7 @@ def run_gpu(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu:
+        os.sched_setaffinity(0, all_cpus)   # the CPU baseline uses every host core
         try:
             v, cores, desc = cpu_chain_rate(spec, kind, seconds=args.cpu_seconds)
             cpu = {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
@@ -592,6 +625,8 @@ def run_gpu(args):
                        "nbits": spec.nbits, "pols": spec.npol, "samples_per_pol_per_block": spec.samples_per_pol,
                        "block_bytes": spec.buffer_size, "form": args.form, "n1": main["n1"], "n2": main["n2"],
                        "diode_period_heaps": spec.diode_period_heaps,
+                       "host_cpus": ("%d CPUs local to the GPU (NVML affinity)" % len(host_cpus)) if host_cpus
+                       else "unbound",
                        "l2": "inputs larger than L2: %d device blocks of %d B rotate (L2 %d B)"
                              % (nrot, spec.buffer_size, l2_bytes),
                        "parallelism": f"replicas x{ws} (one independent stream per GPU)"},
@@ -631,6 +666,7 @@ def run_batch(args):
     _, _, local = dist_env()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    bind_to_gpu_cpus(local, pci_bus_id(dev))   # pinned buffers on the GPU's NUMA node
     import psrdada_cpp_gb300 as G
     from psrdada_cpp_gb300 import synth, autotune
     specs = synth.uneven_streams(16, seed=3)
@@ -777,6 +813,7 @@ def run_serve(args):
     ws, rank = dist_init("nccl")
     _, _, local = dist_env()
     torch.cuda.set_device(local)
+    bind_to_gpu_cpus(local, pci_bus_id(torch.device("cuda", local)))   # pinned buffers on the GPU's NUMA node
     import psrdada_cpp_gb300 as G
     from psrdada_cpp_gb300 import synth, loadgen, autotune
     c1, c3 = synth.config1(), synth.config3()

@@ -50,7 +50,8 @@ cudaError_t launch_tables(uint16_t* parts, float2* w1024, bool bf16, cudaStream_
 }
 
 // The shared-memory image of [B1 | B2 | B3 | W1024] (canonical layout, pad
-// bytes zero) that every tensor-core CTA copies with 16-byte loads.
+// bytes zero; the twiddles as the [c][lane] table of stage_tw) that every
+// tensor-core CTA copies with 16-byte loads.
 __global__ void image_kernel(const uint16_t* parts, const float2* w, uint8_t* img) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < static_cast<int>(kImageBytes); i += gridDim.x * blockDim.x)
     img[i] = 0;
@@ -61,7 +62,7 @@ __global__ void image_kernel(const uint16_t* parts, const float2* w, uint8_t* im
       *reinterpret_cast<uint16_t*>(img + q * kBBytes + kmaj_off(n, k)) = parts[q * 4096 + i];
   }
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < 1024; j += gridDim.x * blockDim.x)
-    reinterpret_cast<float2*>(img + kMaxParts * kBBytes)[j] = w[j];
+    reinterpret_cast<float2*>(img + kMaxParts * kBBytes)[stage_tw(j & 31, j >> 5)] = w[(j & 31) * (j >> 5)];
 }
 
 cudaError_t launch_image(const uint16_t* parts, const float2* w, uint8_t* img, cudaStream_t s) {
@@ -88,7 +89,7 @@ __global__ void __launch_bounds__(128) dft1024_test_kernel(const float2* __restr
   s.bar = bar;
   const int tid = threadIdx.x;
   load_dft32_operand(s.b, g_parts, tid, 128);
-  for (int i = tid; i < 1024; i += 128) w[i] = g_w[i];
+  for (int i = tid; i < 1024; i += 128) w[stage_tw(i & 31, i >> 5)] = g_w[(i & 31) * (i >> 5)];
   const float2* src = in + static_cast<size_t>(blockIdx.x) * 4 * 1024;
   for (int i = tid; i < 4 * 1024; i += 128) xs[i] = src[i];
   if (tid == 0) {

@@ -149,10 +149,17 @@ __device__ __forceinline__ void splitn(float2 v, uint32_t (&p)[SP::n]) {
 struct TileSmem {
   char* a[kMaxParts];   // operand parts, kABytes each (the pass uses SP::n)
   char* b[kMaxParts];   // DFT-32 matrix parts, kBBytes each
-  const float2* w;      // 1024 twiddles W1024^j
+  const float2* w;      // stage twiddles: W1024^(lane*c) at stage_tw(lane, c)
   uint64_t* bar;        // MMA completion barrier
   uint32_t tmem;        // TMEM base (kTmemCols columns)
 };
+
+// The twiddle between the DFT-32 stages of row (t, lane), output c is
+// W1024^(lane*c).  Stored as a [c][lane] table (the 1024 values of W1024 in
+// another order, lane * c < 1024), the 32 lanes that read output c take 32
+// consecutive entries: no bank conflicts, where the natural order W1024[lane*c]
+// made lanes collide in gcd(c, 16) ways.
+__host__ __device__ constexpr int stage_tw(int lane, int c) { return c * 32 + lane; }
 
 // (A part, B part) of the partial products of a stage, smallest first:
 // 6 products (2,0) (0,2) (1,1) (1,0) (0,1) (0,0); 5 products (1,1) (0,2)
@@ -222,7 +229,7 @@ __device__ __forceinline__ bool dft1024_stages(const TileSmem& s, uint32_t& phas
     tmem_ld32(lane_addr, v);
 #pragma unroll
     for (int c = 0; c < 16; ++c) {
-      const float2 z = scale2(cmul(make_float2(v[2 * c], v[2 * c + 1]), s.w[lane * c]), sc2);
+      const float2 z = scale2(cmul(make_float2(v[2 * c], v[2 * c + 1]), s.w[stage_tw(lane, c)]), sc2);
       uint32_t p[SP::n];
       splitn<SP>(z, p);
 #pragma unroll
@@ -232,7 +239,7 @@ __device__ __forceinline__ bool dft1024_stages(const TileSmem& s, uint32_t& phas
     tmem_ld32(lane_addr + 32, v);
 #pragma unroll
     for (int c = 0; c < 16; ++c) {
-      const float2 z = scale2(cmul(make_float2(v[2 * c], v[2 * c + 1]), s.w[lane * (c + 16)]), sc2);
+      const float2 z = scale2(cmul(make_float2(v[2 * c], v[2 * c + 1]), s.w[stage_tw(lane, c + 16)]), sc2);
       uint32_t p[SP::n];
       splitn<SP>(z, p);
 #pragma unroll
