@@ -154,10 +154,18 @@ int gspec_process_device(gspec_handle* h, const void* d_block, size_t used_bytes
 /* One pass of the chain over one block in device memory, accumulated into a
  * caller-owned device output buffer (gspec_info.output_bytes without the
  * saturation record, host layout), on the caller's CUDA stream; updates the
- * baselines.  No handler pipeline, no host copies.  The caller zeroes d_out
- * at the start of an output block.  d_block and d_out are 16-byte aligned
- * (GSPEC_ERR_ARG otherwise). */
+ * baselines.  No handler pipeline, no host copies.  The caller clears d_out
+ * at the start of an output block, with gspec_clear_output_device or by
+ * zeroing all of it.  d_block and d_out are 16-byte aligned (GSPEC_ERR_ARG
+ * otherwise). */
 int gspec_run_block_device(gspec_handle* h, const void* d_block, void* d_out, void* cuda_stream);
+/* Clears an output buffer of h's layout for the first block of an output
+ * block, on the caller's stream (no reference counterpart: the reference
+ * zeroes its accumulators with thrust::fill, edd/detail/GatedSpectrometer.cu):
+ * when each block holds whole outputs (gspec_info.n_blocks == 1) every
+ * spectrum value is stored by the block, so only each record's counters are
+ * zeroed; otherwise the whole buffer. */
+int gspec_clear_output_device(gspec_handle* h, void* d_out, void* cuda_stream);
 
 int gspec_get_info(const gspec_handle* h, gspec_info* info);
 /* Sizes of a handle for cfg without creating it (no reference counterpart):

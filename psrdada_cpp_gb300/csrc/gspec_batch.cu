@@ -14,6 +14,7 @@
 // buffer; runs alternate between them, so the next step's blocks can be
 // copied in while the current step runs.  Later runs replay the
 // instantiated graphs with one launch each.
+#include <algorithm>
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -23,12 +24,16 @@
 
 namespace {
 
-__global__ void batch_phase_kernel(const uint32_t* __restrict__ count, uint32_t n_blocks, uint2* out, uint64_t n_out8,
-                                   uint2* sat, uint64_t n_sat8) {
+// out holds n_rec records of rec8 8-byte words; with one block per output
+// only each record's counters (the words from spec8 on) start from zero, the
+// block stores every spectrum value (gspec_engine::clear_output).
+__global__ void batch_phase_kernel(const uint32_t* __restrict__ count, uint32_t n_blocks, uint2* out, uint64_t n_rec,
+                                   uint64_t rec8, uint64_t spec8, uint2* sat, uint64_t n_sat8) {
   if (*count % n_blocks != 0) return;
   const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
-  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n_out8; i += stride)
-    out[i] = make_uint2(0u, 0u);
+  const uint64_t first = n_blocks == 1 ? spec8 : 0, per = rec8 - first;
+  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n_rec * per; i += stride)
+    out[(i / per) * rec8 + first + i % per] = make_uint2(0u, 0u);
   for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n_sat8; i += stride)
     sat[i] = make_uint2(0u, 0u);
 }
@@ -84,12 +89,14 @@ bool record_step(gspec_batch* b, int slot) {
     cudaStream_t s = b->branch[i];
     if (!bok(b, cudaStreamWaitEvent(s, b->fork, 0), "fork wait")) return false;
     const uint64_t n8 = h->out_bytes / 8, s8 = h->ext_bytes / 8;
-    uint64_t blocks = (n8 + 255) / 256;
+    const uint64_t rec8 = h->rec / 8, spec8 = (h->dual ? 8 : 2) * h->C * 4 / 8;
+    const uint64_t clear8 = h->n_blocks == 1 ? h->n_out * (rec8 - spec8) : n8;
+    uint64_t blocks = (std::max(clear8, s8) + 255) / 256;
     if (blocks > 4ull * b->sm_count) blocks = 4ull * b->sm_count;
     if (blocks < 1) blocks = 1;
     batch_phase_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(
-        b->d_count + i, static_cast<uint32_t>(h->n_blocks), reinterpret_cast<uint2*>(h->d_out[0]), n8,
-        reinterpret_cast<uint2*>(h->d_sat[0]), s8);
+        b->d_count + i, static_cast<uint32_t>(h->n_blocks), reinterpret_cast<uint2*>(h->d_out[0]), h->n_out, rec8,
+        spec8, reinterpret_cast<uint2*>(h->d_sat[0]), s8);
     if (!bok(b, cudaGetLastError(), "phase kernel")) return false;
     if (!bok(b, gspec_engine::run_chain(h, h->d_in[slot], h->d_out[0], h->d_sat[0], s), "chain")) return false;
     batch_count_kernel<<<1, 1, 0, s>>>(b->d_count + i);

@@ -242,6 +242,8 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
   p.flags = h->d_flags;
   p.dev_err = h->d_err;
   p.err_host = h->d_err ? h->h_err_dev : nullptr;   // refreshed by the block's finalisation
+  // each block holds whole outputs: every spectrum value is written once per block
+  p.store = h->n_blocks == 1 ? 1u : 0u;
   const int N = static_cast<int>(h->cfg.fft_length);
   cudaError_t e;
   // gate masks per item and the gates each frame holds data in
@@ -284,8 +286,6 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
     f.njobs = h->d_njobs;
     f.dc = h->d_dc;
     f.dcsum = h->d_dcsum;
-    // each block holds whole outputs: the caller's zeroed bins take exactly one scatter
-    f.store_bins = h->n_blocks == 1 ? 1u : 0u;
     // job lists of every output spectrum of the block
     f.k0 = 0;
     f.nk = static_cast<uint32_t>(h->n_out);
@@ -386,7 +386,7 @@ int do_process(gspec_handle* h, const void* block, size_t used, gspec_output* ou
     if (!cuda_ok(h, cudaStreamSynchronize(h->d2h), "D2H")) return GSPEC_ERR_CUDA;
     h->oa ^= 1;
     h->ha ^= 1;
-    if (!cuda_ok(h, cudaMemsetAsync(h->d_out[h->oa], 0, h->out_bytes, h->proc), "zero output") ||
+    if (!cuda_ok(h, gspec_engine::clear_output(h, h->d_out[h->oa], h->proc), "clear output") ||
         !cuda_ok(h, cudaMemsetAsync(h->d_sat[h->oa], 0, h->ext_bytes, h->proc), "zero saturation"))
       return GSPEC_ERR_CUDA;
   }
@@ -446,6 +446,18 @@ int do_process(gspec_handle* h, const void* block, size_t used, gspec_output* ou
 }  // namespace
 
 namespace gspec_engine {
+
+// What an output buffer needs cleared before the first block of an output
+// block: with one block per output every spectrum value is stored by that
+// block (ChainParams::store), so only each record's counters (added to by
+// the block's atomics); otherwise the whole buffer.
+cudaError_t clear_output(const gspec_handle* h, uint8_t* d_out, cudaStream_t s) {
+  if (h->n_blocks == 1) {
+    const uint64_t spectra = (h->dual ? 8 : 2) * h->C * 4;
+    return cudaMemset2DAsync(d_out + spectra, h->rec, 0, h->rec - spectra, h->n_out, s);
+  }
+  return cudaMemsetAsync(d_out, 0, h->out_bytes, s);
+}
 
 bool configure_handle(gspec_handle* h) { return configure(h); }
 
@@ -714,6 +726,14 @@ int gspec_process(gspec_handle* h, const char* block, size_t used_bytes, gspec_o
 
 int gspec_process_device(gspec_handle* h, const void* d_block, size_t used_bytes, gspec_output* out) {
   return do_process(h, d_block, used_bytes, out, true);
+}
+
+int gspec_clear_output_device(gspec_handle* h, void* d_out, void* cuda_stream) {
+  if (!h || !d_out) return GSPEC_ERR_ARG;
+  return cuda_ok(h, gspec_engine::clear_output(h, static_cast<uint8_t*>(d_out), static_cast<cudaStream_t>(cuda_stream)),
+                 "clear output")
+             ? GSPEC_OK
+             : GSPEC_ERR_CUDA;
 }
 
 int gspec_run_block_device(gspec_handle* h, const void* d_block, void* d_out, void* cuda_stream) {

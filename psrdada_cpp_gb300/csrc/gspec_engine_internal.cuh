@@ -91,6 +91,9 @@ bool plan_handle(gspec_handle* h);
 uint64_t footprint(const gspec_handle* h);
 uint64_t bsum_bytes(const gspec_handle* h);
 void fill_info(const gspec_handle* h, gspec_info* info);
+// Clears an output buffer of h's layout for the first block of an output
+// block (only the counters when each block holds whole outputs).
+cudaError_t clear_output(const gspec_handle* h, uint8_t* d_out, cudaStream_t s);
 // Enqueues the whole chain for one block on stream s using h's buffers.
 cudaError_t run_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out, unsigned long long* d_sat,
                       cudaStream_t s);

@@ -494,7 +494,7 @@ cudaError_t launch_fourstep(int N, int nbits, bool dual, const FourStepParams& p
   if (pass == 2) {
     const int vals = dual ? 8 : 2;
     fourstep_scatter_kernel<<<dim3(p.N1 / 32, (p.N2 / 2 + 1 + 31) / 32, p.nk * vals), dim3(32, 8), 0, s>>>(
-        p, vals, p.store_bins ? 1 : 0);
+        p, vals, p.c.store ? 1 : 0);
     return cudaGetLastError();
   }
   if (p.form != 0 && ((pass == 0 && p.N1 == 1024) || (pass == 1 && p.N2 == 1024)))

@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS, GSPEC_SMALL_MINB)
 #pragma unroll 4
     for (int s = 0; s < Cfg::NSLOT; ++s) v += acc[s * Cfg::VALS * C + i];
     if (p.slices == 1) {
-      outf[i] += v;
+      outf[i] = p.store ? v : outf[i] + v;
     } else {
       p.partial[(static_cast<size_t>(k) * p.slices + sl) * Cfg::VALS * C + i] = v;
     }
@@ -411,7 +411,7 @@ __global__ void reduce_finalize_kernel(ChainParams p, int vals_c, int npol, int 
     float v = 0.f;
     const float* src = p.partial + static_cast<size_t>(k) * p.slices * vals_c + i;
     for (uint32_t s = 0; s < p.slices; ++s) v += src[static_cast<size_t>(s) * vals_c];
-    outf[i] += v;
+    outf[i] = p.store ? v : outf[i] + v;
   }
   if (blockIdx.x == gridDim.x - 1 && blockIdx.y == gridDim.y - 1)
     finalize_block(p, npol, C, dual, convention, ungated, baselines_out);

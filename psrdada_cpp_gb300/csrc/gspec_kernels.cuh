@@ -30,6 +30,8 @@ struct ChainParams {
   uint32_t frames_per_unit;
   uint32_t* dev_err;               // set non-zero when a bounded device wait gives up
   volatile uint32_t* err_host;     // page-locked mirror of *dev_err written by the finalisation (or null)
+  uint32_t store;                  // 1: one block per output, so each launch writes every spectrum value of
+                                   // its records (stores, no read-add); only the counters start from zero
 };
 
 // Large-N (four-step) parameters.
@@ -48,8 +50,6 @@ struct FourStepParams {
   uint32_t* dc;                    // [n_out][2] frames without data per gate
   unsigned long long* dcsum;       // [n_out][maxjobs][6] exact DC sums of each job (see exact_dc)
   float* bsum;                     // pass B row-pair sums of the launch: [nk][N1/2][VALS][N2 + 1]
-  uint32_t store_bins;             // 1: the launch holds every contribution to its spectra (one block
-                                   // per output), so the scatter writes the bins instead of adding
   // tensor-core form (form != 0): DFT-32 operand parts and W1024 twiddles
   uint32_t form;                   // GSPEC_FORM_*
   const uint4* tc_img;             // [B1 | B2 | B3 | W1024] in shared-memory layout

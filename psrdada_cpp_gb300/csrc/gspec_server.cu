@@ -263,7 +263,7 @@ bool issue(gspec_server* s, Stream& st, const Queued& q, int obuf) {
   if (first) {
     // the accumulator's previous D2H must be done before it is cleared
     if (!ok(st, cudaStreamWaitEvent(h->proc, st.ev_out_done[oi], 0), "wait D2H") ||
-        !ok(st, cudaMemsetAsync(h->d_out[oi], 0, h->out_bytes, h->proc), "clear output") ||
+        !ok(st, gspec_engine::clear_output(h, h->d_out[oi], h->proc), "clear output") ||
         !ok(st, cudaMemsetAsync(h->d_sat[oi], 0, h->ext_bytes, h->proc), "clear saturation"))
       return false;
   }

@@ -94,6 +94,7 @@ def load_library() -> ctypes.CDLL:
     lib.gspec_process.argtypes = [vp, vp, sz, ctypes.POINTER(GspecOutput)]
     lib.gspec_process_device.argtypes = [vp, vp, sz, ctypes.POINTER(GspecOutput)]
     lib.gspec_run_block_device.argtypes = [vp, vp, vp, vp]
+    lib.gspec_clear_output_device.argtypes = [vp, vp, vp]
     lib.gspec_get_info.argtypes = [vp, ctypes.POINTER(GspecInfo)]
     lib.gspec_last_error.restype = ctypes.c_char_p
     lib.gspec_last_error.argtypes = [vp]
@@ -329,6 +330,11 @@ class GatedSpectrometer:
         out = (ctypes.c_uint64 * (2 * n))()
         self._check(self._lib.gspec_get_saturation(self._h, out))
         return np.frombuffer(out, dtype=np.uint64).reshape(n, 2).copy()
+
+    def clear_output_device(self, d_out: int, stream: int = 0) -> None:
+        """Clears a device output buffer for the first block of an output block
+        (only the counters when each block holds whole outputs)."""
+        self._check(self._lib.gspec_clear_output_device(self._h, ctypes.c_void_p(d_out), ctypes.c_void_p(stream)))
 
     def run_block_device(self, d_block: int, d_out: int, stream: int = 0) -> None:
         self._check(self._lib.gspec_run_block_device(self._h, ctypes.c_void_p(d_block), ctypes.c_void_p(d_out),

@@ -202,11 +202,13 @@ def run_alone_device(spec, blocks):
                              input_type=G.DUAL_POL if spec.dual_pol else G.SINGLE_POL,
                              flags=G.FLAG_NO_HOST_BUFFERS) as gs:
         info = gs.info()
-        d_out = torch.zeros(int(info.output_bytes), dtype=torch.uint8, device=dev)
+        # garbage first: the caller's clear (counters only when a block holds whole outputs)
+        # must be all the buffer needs
+        d_out = torch.full((int(info.output_bytes),), 0x5A, dtype=torch.uint8, device=dev)
         s = torch.cuda.current_stream(dev).cuda_stream
         for i, blk in enumerate(blocks):
             if i % int(info.n_blocks) == 0:
-                d_out.zero_()
+                gs.clear_output_device(d_out.data_ptr(), s)
             d_blk = torch.from_numpy(blk).to(dev)
             gs.run_block_device(d_blk.data_ptr(), d_out.data_ptr(), s)
             if (i + 1) % int(info.n_blocks) == 0:
