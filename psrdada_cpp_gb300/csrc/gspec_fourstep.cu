@@ -20,7 +20,9 @@
 namespace gspec {
 
 
-// One thread per output spectrum of the launch: its job list.
+// One thread per output spectrum of the launch: its job list (frame order:
+// the two gate jobs of a frame are neighbours, so pass A's CTAs that read the
+// same frame run close together).
 __global__ void fourstep_plan_kernel(FourStepParams p, int dual) {
   const uint32_t kk = blockIdx.x * blockDim.x + threadIdx.x;
   if (kk >= p.nk) return;
@@ -196,6 +198,12 @@ struct PassBCfg {
   static constexpr int J = THREADS / JOB_THREADS;    // jobs transformed together
   static constexpr int STRIDE = spad_size(N2);
   static constexpr int VALS = DUAL ? 8 : 2;
+  // dual pol at 1024-point rows: the CTA visits the spectrum's gate-0 jobs,
+  // then its gate-1 jobs (a permutation in shared memory), so a thread holds
+  // one gate's I, Q, U, V per bin at a time: half the bin sums, 157 instead
+  // of 204 registers, three CTAs per SM
+  static constexpr bool BANK = DUAL && N2 == 1024;
+  static constexpr int HELD = BANK ? 4 : VALS;   // values a thread sums per bin at a time
   static constexpr int BPT = (N2 + 1 + THREADS - 1) / THREADS;   // output bins per thread
   static constexpr int STAGE_F2 = J * 2 * N2;        // one TMA stage: J jobs x 2 rows, unpadded
   static constexpr size_t STAGE_BYTES = static_cast<size_t>(STAGE_F2) * sizeof(float2);
@@ -204,6 +212,8 @@ struct PassBCfg {
   static constexpr size_t JW_BYTES = ((J * sizeof(uint32_t)) + 15) / 16 * 16;
   static constexpr int NST = GSPEC_PASSB_STAGES;     // TMA stages: NST - 1 groups ahead
   static constexpr size_t SMEM = NST * STAGE_BYTES + WORK_BYTES + TW_BYTES + JW_BYTES + NST * sizeof(uint64_t);
+  // resident CTAs the register allocation is sized for
+  static constexpr int MINB = BANK ? 3 : GSPEC_PASSB_MINB;
 };
 
 
@@ -215,7 +225,7 @@ struct PassBCfg {
 // sums in registers over all jobs of the spectrum, adding the jobs in
 // order, so the result does not depend on scheduling.
 template <int N2, bool DUAL>
-__global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, GSPEC_PASSB_MINB) fourstep_b_kernel(FourStepParams p) {
+__global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, PassBCfg<N2, DUAL>::MINB) fourstep_b_kernel(FourStepParams p) {
   using Cfg = PassBCfg<N2, DUAL>;
   constexpr int J = Cfg::J;
   constexpr int BPT = Cfg::BPT;
@@ -247,11 +257,31 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, GSPEC_PASSB_MINB)
   const uint32_t njobs = p.njobs[k];
   const uint32_t* jobs = p.jobs + k * p.maxjobs;
   const uint32_t ngroups = (njobs + J - 1) / J;
+  // BANK: the spectrum's job words and the visiting order (gate-0 jobs, then
+  // gate-1 jobs, each in list order) after the barriers, [maxjobs] each
+  uint32_t* words = reinterpret_cast<uint32_t*>(bar + NST);
+  uint32_t* order = words + p.maxjobs;
+  if constexpr (Cfg::BANK) {
+    for (uint32_t i = tid; i < njobs; i += Cfg::THREADS) words[i] = jobs[i];
+    __syncthreads();
+  }
   if (tid == 0) {
 #pragma unroll
     for (int i = 0; i < NST; ++i) mbar_init(&bar[i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if constexpr (Cfg::BANK) {
+      uint32_t w = 0;
+      for (uint32_t i = 0; i < njobs; ++i)
+        if (job_ga(words[i]) == 0) order[w++] = i;
+      for (uint32_t i = 0; i < njobs; ++i)
+        if (job_ga(words[i]) != 0) order[w++] = i;
+    }
   }
+  // list position of the i-th job this CTA visits
+  auto slot_of = [&](uint32_t i) -> uint32_t {
+    if constexpr (Cfg::BANK) return order[i];
+    else return i;
+  };
   load_twiddles<N2>(tws, p.tw2);
   __syncthreads();
   // thread 0: rows of job group g into stage s
@@ -260,7 +290,7 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, GSPEC_PASSB_MINB)
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     mbar_expect_tx(&bar[s], nq * 2 * kRowBytes);
     for (uint32_t qq = 0; qq < nq; ++qq) {
-      const float2* seq = p.scratch + (static_cast<size_t>(kk) * p.maxjobs + g * J + qq) * N;
+      const float2* seq = p.scratch + (static_cast<size_t>(kk) * p.maxjobs + slot_of(g * J + qq)) * N;
       float2* dst = stage + static_cast<size_t>(s) * Cfg::STAGE_F2 + qq * 2 * N2;
       bulk_g2s(dst, seq + static_cast<size_t>(rowA) * N2, kRowBytes, &bar[s]);
       bulk_g2s(dst + N2, seq + static_cast<size_t>(rowB) * N2, kRowBytes, &bar[s]);
@@ -271,12 +301,22 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, GSPEC_PASSB_MINB)
 
   // job words one group ahead: the global load of group g + 1 is in flight
   // while group g is transformed
-  uint32_t next_job = (tid < J && static_cast<uint32_t>(tid) < njobs) ? jobs[tid] : 0u;
-  float acc[BPT][VALS];
+  auto job_at = [&](uint32_t i) -> uint32_t {
+    if constexpr (Cfg::BANK) return words[order[i]];
+    else return jobs[i];
+  };
+  uint32_t next_job = (tid < J && static_cast<uint32_t>(tid) < njobs) ? job_at(tid) : 0u;
+  constexpr int HELD = Cfg::HELD;
+  float acc[BPT][HELD];
 #pragma unroll
   for (int i = 0; i < BPT; ++i)
 #pragma unroll
-    for (int v = 0; v < VALS; ++v) acc[i][v] = 0.f;
+    for (int v = 0; v < HELD; ++v) acc[i][v] = 0.f;
+  // row-pair sums, contiguous in the slot a (coalesced); fourstep_scatter_kernel
+  // moves them into the output bins, whose index c strides by N1 along a.
+  // Value v of slot a at bs[v * (N2 + 1) + a]; dual pol: v = 2 * stokes + gate.
+  float* bs = p.bsum + static_cast<size_t>(blockIdx.x) * VALS * (N2 + 1);
+  uint32_t cur = 0;   // BANK: the gate whose sums acc holds
 
   for (uint32_t g = 0; g < ngroups; ++g) {
     const int s = static_cast<int>(g % NST);
@@ -297,12 +337,22 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, GSPEC_PASSB_MINB)
     const int nq = static_cast<int>(min(static_cast<uint32_t>(J), njobs - j0));
     const bool active = q < nq;
     if (tid < nq) jw[tid] = next_job;
-    if (tid < J && j0 + J + tid < njobs) next_job = jobs[j0 + J + tid];
+    if (tid < J && j0 + J + tid < njobs) next_job = job_at(j0 + J + tid);
     {
       const int r = lt / Cfg::T2;
       const int t = lt - r * Cfg::T2;
       fft_smem_from<N2, 16>(stage + static_cast<size_t>(s) * Cfg::STAGE_F2 + (q * 2 + r) * N2,
                             work + (2 * q + r) * Cfg::STRIDE, tws, t, active);
+    }
+    // BANK: the group's first job of gate 1, where gate 0's sums are complete
+    int qb = nq;
+    if constexpr (Cfg::BANK) {
+      if (cur == 0)
+        for (int qq = 0; qq < nq; ++qq)
+          if (job_ga(jw[qq]) != 0) {
+            qb = qq;
+            break;
+          }
     }
 #pragma unroll
     for (int i = 0; i < BPT; ++i) {
@@ -314,43 +364,65 @@ __global__ void __launch_bounds__(PassBCfg<N2, DUAL>::THREADS, GSPEC_PASSB_MINB)
         const uint32_t job = jw[qq];
         const float2 za = work[(2 * qq + r) * Cfg::STRIDE + spad(k2)];
         const float2 zb = work[(2 * qq + pr) * Cfg::STRIDE + spad(k2p)];
-        accumulate_bin<DUAL>(acc[i], za, zb, job);
+        if constexpr (Cfg::BANK) {
+          if (qq == qb) {
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+              bs[(2 * v) * (N2 + 1) + a] = acc[i][v];
+              acc[i][v] = 0.f;
+            }
+          }
+          accumulate_stokes(acc[i], za, zb);
+        } else {
+          accumulate_bin<DUAL>(acc[i], za, zb, job);
+        }
       }
     }
+    if (Cfg::BANK && qb < nq) cur = 1;
     __syncthreads();
   }
-  // bin 0 from the exact per-job sums (exact_dc), over the jobs in order;
-  // the work buffer is free after the loop's last barrier
-  if (rp == 0)
-    exact_dc_bin<DUAL>(p, k, reinterpret_cast<float*>(work),
-                       static_cast<uint32_t>(Cfg::WORK_BYTES / (VALS * sizeof(float))), acc[0]);
-  // gates without data: constant baseline in bin 0 (row pair 0, slot a = 0)
-  if (rp == 0 && tid == 0) {
-    const float n = static_cast<float>(N);
-    for (int gate = 0; gate < 2; ++gate) {
-      const float cnt = static_cast<float>(p.dc[2 * k + gate]);
-      if (cnt == 0.f) continue;
-      if constexpr (!DUAL) {
-        const float d = n * p.c.baselines[gate];
-        acc[0][gate] += cnt * d * d;
-      } else {
-        const float x = n * p.c.baselines[gate], y = n * p.c.baselines[2 + gate];
-        acc[0][0 + gate] += cnt * (x * x + y * y);
-        acc[0][2 + gate] += cnt * (x * x - y * y);
-        acc[0][4 + gate] += cnt * (2.f * x * y);
-      }
-    }
-  }
-  // row-pair sums, contiguous in the slot a (coalesced); fourstep_scatter_kernel
-  // adds them into the output bins, whose index c strides by N1 along a
-  float* bs = p.bsum + static_cast<size_t>(blockIdx.x) * VALS * (N2 + 1);
-  (void)C;
+  // the sums held at the end (BANK: gate `cur`; a gate without jobs sums to 0)
 #pragma unroll
   for (int i = 0; i < BPT; ++i) {
     const int a = tid + i * Cfg::THREADS;
     if (a >= nbins) continue;
+    if constexpr (Cfg::BANK) {
 #pragma unroll
-    for (int v = 0; v < VALS; ++v) bs[v * (N2 + 1) + a] = acc[i][v];
+      for (int v = 0; v < 4; ++v) {
+        bs[(2 * v + cur) * (N2 + 1) + a] = acc[i][v];
+        if (cur == 0) bs[(2 * v + 1) * (N2 + 1) + a] = 0.f;
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < VALS; ++v) bs[v * (N2 + 1) + a] = acc[i][v];
+    }
+  }
+  (void)C;
+  // bin 0 (row pair 0, slot 0, thread 0) from the exact per-job sums
+  // (exact_dc), over the jobs in order, plus the constant baseline of gates
+  // without data; the work buffer is free after the loop's last barrier
+  if (rp == 0) {
+    float c0[VALS];
+    exact_dc_bin<DUAL>(p, k, reinterpret_cast<float*>(work),
+                       static_cast<uint32_t>(Cfg::WORK_BYTES / (VALS * sizeof(float))), c0);
+    if (tid == 0) {
+      const float n = static_cast<float>(N);
+      for (int gate = 0; gate < 2; ++gate) {
+        const float cnt = static_cast<float>(p.dc[2 * k + gate]);
+        if (cnt == 0.f) continue;
+        if constexpr (!DUAL) {
+          const float d = n * p.c.baselines[gate];
+          c0[gate] += cnt * d * d;
+        } else {
+          const float x = n * p.c.baselines[gate], y = n * p.c.baselines[2 + gate];
+          c0[0 + gate] += cnt * (x * x + y * y);
+          c0[2 + gate] += cnt * (x * x - y * y);
+          c0[4 + gate] += cnt * (2.f * x * y);
+        }
+      }
+#pragma unroll
+      for (int v = 0; v < VALS; ++v) bs[v * (N2 + 1)] = c0[v];
+    }
   }
 }
 
@@ -455,11 +527,11 @@ template <int N2, bool DUAL>
 static cudaError_t launch_b_n2(const FourStepParams& p, cudaStream_t s) {
   using Cfg = PassBCfg<N2, DUAL>;
   const unsigned grid = p.nk * (p.N1 / 2);
+  const size_t smem = Cfg::SMEM + (Cfg::BANK ? 2 * static_cast<size_t>(p.maxjobs) * sizeof(uint32_t) : 0);
   auto kern = fourstep_b_kernel<N2, DUAL>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(Cfg::SMEM));
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   if (e != cudaSuccess) return e;
-  kern<<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(p);
+  kern<<<grid, Cfg::THREADS, smem, s>>>(p);
   return cudaGetLastError();
 }
 

@@ -164,6 +164,19 @@ __device__ __forceinline__ float2 exact_dc(const FourStepParams& p, uint32_t k, 
 // job's contribution is formed by one thread into `scratch` (at most `cap`
 // jobs at a time) and thread 0 adds them into acc0 in job order, which gives
 // the same sums as adding the jobs one after the other.
+// Stokes I, Q, U, V of one dual-pol job's bin (accumulate_bin without the
+// gate selection) added to acc: the caller holds one gate's sums at a time.
+__device__ __forceinline__ void accumulate_stokes(float (&acc)[4], float2 za, float2 zb) {
+  const float p1x = 0.5f * (za.x + zb.x), p1y = 0.5f * (za.y - zb.y);
+  const float p2x = 0.5f * (za.y + zb.y), p2y = -0.5f * (za.x - zb.x);
+  const float a1 = fmaf(p1x, p1x, p1y * p1y);
+  const float a2 = fmaf(p2x, p2x, p2y * p2y);
+  acc[0] += a1 + a2;
+  acc[1] += a1 - a2;
+  acc[2] += 2.f * fmaf(p1x, p2x, p1y * p2y);
+  acc[3] += -2.f * fmaf(p1y, p2x, -p1x * p2y);
+}
+
 template <bool DUAL, int VALS>
 __device__ __forceinline__ void exact_dc_bin(const FourStepParams& p, uint32_t k, float* scratch, uint32_t cap,
                                              float (&acc0)[VALS]) {
