@@ -532,7 +532,7 @@ uint64_t footprint(const gspec_handle* h) {
   t += 2 * (sz(h->cfg.buffer_size) + sz(h->out_bytes) + sz(h->ext_bytes));
   t += sz(h->ext_bytes) + sz(4 * sizeof(float)) + sz(2 * kPolStats * sizeof(unsigned long long)) + sz(sizeof(uint32_t));
   if (h->path == 0) {
-    t += sz(tw_size(static_cast<int>(N)) * sizeof(float2));
+    t += sz(small_tw_size(static_cast<int>(N)) * sizeof(float2));
     if (h->slices > 1) t += sz(h->n_out * h->slices * vals * h->C * sizeof(float));
   } else {
     t += sz(tw_size(static_cast<int>(h->N1)) * sizeof(float2)) + sz(tw_size(static_cast<int>(h->N2)) * sizeof(float2));
@@ -642,7 +642,7 @@ gspec_handle* gspec_create(const gspec_config* cfg, char* err, size_t err_len) {
     return bail("");
   cudaMemset(h->d_err, 0, sizeof(uint32_t));
   if (h->path == 0) {
-    if (!dalloc(h, &h->d_tw, tw_size(N) * sizeof(float2), "twiddles")) return bail("");
+    if (!dalloc(h, &h->d_tw, small_tw_size(N) * sizeof(float2), "twiddles")) return bail("");
     if (!cuda_ok(h, launch_twiddles(N, h->d_tw, h->proc), "twiddles")) return bail("");
     if (h->slices > 1 &&
         !dalloc(h, &h->d_partial, h->n_out * h->slices * vals * h->C * sizeof(float), "partials"))

@@ -292,6 +292,203 @@ __global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS, GSPEC_SMALL_MINB)
   commit_stats<NPOL>(p, st, k, Cfg::VALS * C, red);
 }
 
+// ------------------------------------------------------------ warp chain
+// Single-pol 1024-point chain with one FFT per warp (N = 32 x 32).  Lane l
+// unpacks and gates the 32 consecutive samples 32 l .. 32 l + 31 of each of
+// the job's two frames (one item lookup per span, as in the shared-memory
+// chain) into two padded 32 x 33 float planes of the warp's tile; reading
+// them back by column leaves z[32 j + l] (j = 0..31) in lane l.  A DFT-32
+// over j in registers, a multiply by W1024^(l k1), and a transpose through
+// the same tile give lane k1 row k1 for the second DFT-32: lane k1 ends with
+// Z(k1 + 32 k2), k2 = 0..31, and the mirror Z(N - c) of its bin c comes
+// from lane (32 - k1) mod 32 by one shuffle.  A warp works through its
+// jobs on its own (no block barrier in the job loop), holding its bins'
+// power sums in registers; the warps' sums are added in a fixed order at the
+// end, so results do not depend on scheduling.
+
+// W32^c = exp(-2 pi i c / 32), c = 0..15, from cos/sin of pi/16, pi/8, 3 pi/16, pi/4
+constexpr float kC16 = 0.98078528040323044913f, kS16 = 0.19509032201612826785f;   // cos, sin pi/16
+constexpr float kC316 = 0.83146961230254523708f, kS316 = 0.55557023301960222474f; // cos, sin 3pi/16
+__device__ __forceinline__ float2 w32(int c) {
+  switch (c) {
+    case 1: return make_float2(kC16, -kS16);
+    case 2: return make_float2(kC8, -kS8);
+    case 3: return make_float2(kC316, -kS316);
+    case 4: return make_float2(kS2, -kS2);
+    case 5: return make_float2(kS316, -kC316);
+    case 6: return make_float2(kS8, -kC8);
+    case 7: return make_float2(kS16, -kC16);
+    case 9: return make_float2(-kS16, -kC16);
+    case 10: return make_float2(-kS8, -kC8);
+    case 11: return make_float2(-kS316, -kC316);
+    case 12: return make_float2(-kS2, -kS2);
+    case 13: return make_float2(-kC316, -kS316);
+    case 14: return make_float2(-kC8, -kS8);
+    default: return make_float2(-kC16, -kS16);   // 15
+  }
+}
+
+// Forward DFT-32 in registers, natural order in and out: DFT-16 of the even
+// and the odd samples, then X[c] = E[c] + W32^c O[c], X[c + 16] = E[c] - W32^c O[c].
+__device__ __forceinline__ void dft32(float2 (&v)[32]) {
+  float2 e[16], o[16];
+#pragma unroll
+  for (int b = 0; b < 16; ++b) {
+    e[b] = v[2 * b];
+    o[b] = v[2 * b + 1];
+  }
+  dft16(e);
+  dft16(o);
+#pragma unroll
+  for (int c = 0; c < 16; ++c) {
+    const float2 t = c == 0 ? o[0] : (c == 8 ? cmul_mi(o[8]) : cmul(o[c], w32(c)));
+    v[c] = cadd(e[c], t);
+    v[c + 16] = csub(e[c], t);
+  }
+}
+
+struct WarpChainCfg {
+  static constexpr int N = 1024, C = N / 2 + 1;
+  static constexpr int WARPS = 8, THREADS = 32 * WARPS;
+  static constexpr int TILE = 32 * 33;                                  // float2 per warp tile
+  static constexpr size_t TILE_BYTES = static_cast<size_t>(WARPS) * TILE * sizeof(float2);
+  static constexpr size_t TW_BYTES = 1024 * sizeof(float2);
+  static constexpr int MAX_JOBS = 2 * kMaxUnitFrames;
+  static constexpr size_t JOB_BYTES = (MAX_JOBS + 4) * sizeof(uint32_t);
+  static constexpr size_t RED_BYTES = WARPS * 12 * sizeof(unsigned long long);
+  static constexpr size_t SMEM = TILE_BYTES + TW_BYTES + JOB_BYTES + RED_BYTES;
+  static_assert(static_cast<size_t>(WARPS) * 2 * C * sizeof(float) <= TILE_BYTES, "warp sums fit the tiles");
+};
+
+template <int NBITS>
+__global__ void __launch_bounds__(WarpChainCfg::THREADS, 2) warp_chain_kernel(ChainParams p) {
+  using Cfg = WarpChainCfg;
+  constexpr int N = Cfg::N, C = Cfg::C;
+  extern __shared__ float4 smem_f4[];
+  char* base = reinterpret_cast<char*>(smem_f4);
+  float2* tiles = reinterpret_cast<float2*>(base);
+  float2* tw = reinterpret_cast<float2*>(base + Cfg::TILE_BYTES);                 // [k1][lane]
+  uint32_t* jobs = reinterpret_cast<uint32_t*>(base + Cfg::TILE_BYTES + Cfg::TW_BYTES);
+  uint32_t* jinfo = jobs + Cfg::MAX_JOBS;   // [0] njobs, [1] dc gate 0, [2] dc gate 1
+  unsigned long long* red =
+      reinterpret_cast<unsigned long long*>(base + Cfg::TILE_BYTES + Cfg::TW_BYTES + Cfg::JOB_BYTES);
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t unit = blockIdx.x;
+  const uint32_t k = unit / p.slices;
+  const uint32_t sl = unit - k * p.slices;
+  const uint32_t f0 = k * p.nacc + sl * p.frames_per_unit;
+  if (tid == 0) {
+    uint32_t dc[2];
+    jinfo[0] = build_jobs(p.flags + f0, p.frames_per_unit, false, jobs, dc);
+    jinfo[1] = dc[0];
+    jinfo[2] = dc[1];
+  }
+  // the stage twiddles W1024^(lane k1) follow the Stockham tables of N
+  for (int i = tid; i < 1024; i += Cfg::THREADS) tw[i] = __ldg(p.tw + tw_size(N) + i);
+  const float b0 = p.baselines[0], b1 = p.baselines[1];
+  __syncthreads();
+  const uint32_t njobs = jinfo[0];
+  GateStats st;
+  float acc0[17], acc1[17];
+#pragma unroll
+  for (int i = 0; i < 17; ++i) acc0[i] = acc1[i] = 0.f;
+  float2* T = tiles + warp * Cfg::TILE;
+
+  for (uint32_t jx = warp; jx < njobs; jx += Cfg::WARPS) {
+    const uint32_t job = jobs[jx];
+    const uint32_t fa = job_fa(job), ga = job_ga(job), fb = job_fb(job), gb = job_gb(job);
+    const bool has_b = fb != kNoFrame;
+    const float ba = ga ? b1 : b0, bb = gb ? b1 : b0;
+    // frame a (gate ga) into the re plane, frame b (gate gb; a job of one
+    // frame with data in both gates has fb == fa) into the im plane
+    float* Tre = reinterpret_cast<float*>(T);
+    float* Tim = Tre + 32 * 33;
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+      float v[32];
+      if (h == 0 || has_b) {
+        const uint32_t s0 = (f0 + (h ? fb : fa)) * N + 32 * lane;
+        gate_group1<NBITS, 32>(p.g, 0, s0, h ? bb : ba, h ? gb : ga, v, st, true);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) v[j] = 0.f;
+      }
+      float* P = h ? Tim : Tre;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) P[lane * 33 + j] = v[j];
+    }
+    __syncwarp();
+    float2 x[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) x[j] = make_float2(Tre[j * 33 + lane], Tim[j * 33 + lane]);
+    __syncwarp();
+    // DFT-32 over j; twiddle W1024^(lane k1); transpose through the warp's tile
+    dft32(x);
+#pragma unroll
+    for (int k1 = 1; k1 < 32; ++k1) x[k1] = cmul(x[k1], tw[k1 * 32 + lane]);
+#pragma unroll
+    for (int k1 = 0; k1 < 32; ++k1) T[k1 * 33 + lane] = x[k1];
+    __syncwarp();
+#pragma unroll
+    for (int n2 = 0; n2 < 32; ++n2) x[n2] = T[lane * 33 + n2];
+    __syncwarp();
+    // DFT-32 over n2: lane k1 holds Z(k1 + 32 k2) in x[k2]
+    dft32(x);
+    // bins c = lane + 32 k2 <= N/2, the mirror Z(N - c) from lane (32 - lane) mod 32
+    // (lane 0: its own x[(32 - k2) mod 32]); A = (Z(c) + conj Z(N-c))/2, B = (Z(c) - conj Z(N-c))/(2i)
+    const int partner = (32 - lane) & 31;
+#pragma unroll
+    for (int k2 = 0; k2 < 17; ++k2) {
+      const float2 src = x[31 - (k2 & 15) - (k2 >> 4) * 16];
+      float2 b = make_float2(__shfl_sync(0xffffffffu, src.x, partner), __shfl_sync(0xffffffffu, src.y, partner));
+      if (lane == 0) b = x[(32 - k2) & 31];
+      if (k2 == 16 && lane != 0) continue;
+      const float2 a = x[k2];
+      const float sx = a.x + b.x, sy = a.y - b.y;
+      const float dx = a.x - b.x, dy = a.y + b.y;
+      const float pa = 0.25f * fmaf(sx, sx, sy * sy);
+      const float pb = has_b ? 0.25f * fmaf(dx, dx, dy * dy) : 0.f;
+      acc0[k2] += (ga == 0 ? pa : 0.f) + (gb == 0 ? pb : 0.f);
+      acc1[k2] += (ga != 0 ? pa : 0.f) + (gb != 0 ? pb : 0.f);
+    }
+  }
+  __syncthreads();
+  // the warps' sums, then their fixed-order total; the tiles are free now
+  float* wsum = reinterpret_cast<float*>(tiles);   // [warp][2][C]
+#pragma unroll
+  for (int k2 = 0; k2 < 17; ++k2) {
+    const int c = lane + 32 * k2;
+    if (c > N / 2) continue;
+    wsum[(warp * 2 + 0) * C + c] = acc0[k2];
+    wsum[(warp * 2 + 1) * C + c] = acc1[k2];
+  }
+  __syncthreads();
+  float* outf = reinterpret_cast<float*>(p.out + k * p.out_rec);
+  const float n = static_cast<float>(N);
+  for (int i = tid; i < 2 * C; i += Cfg::THREADS) {
+    float v = 0.f;
+#pragma unroll
+    for (int w = 0; w < Cfg::WARPS; ++w) v += wsum[w * 2 * C + i];
+    // gates without data in a frame: constant baseline, bin 0 only
+    if (i == 0 || i == C) {
+      const int gate = i == 0 ? 0 : 1;
+      const float cnt = static_cast<float>(jinfo[1 + gate]);
+      if (cnt != 0.f) {
+        const float d = n * (gate ? b1 : b0);
+        v += cnt * d * d;
+      }
+    }
+    if (p.slices == 1) {
+      outf[i] = p.store ? v : outf[i] + v;
+    } else {
+      p.partial[(static_cast<size_t>(k) * p.slices + sl) * 2 * C + i] = v;
+    }
+  }
+  GateStats sts[1] = {st};
+  commit_stats<1>(p, sts, k, 2 * C, red);
+}
+
 // Pre-pass of a block: the gate masks of every side-channel item index of
 // one pol (dual: merged items; bit0 gate 0, bit1 gate 1), and per frame the
 // gates holding at least one sample.  The items a frame touches are
@@ -543,7 +740,26 @@ size_t small_fft_smem(int N, bool dual) {
   return s;
 }
 
+template <int NBITS>
+static cudaError_t launch_warp_chain_t(const ChainParams& p, cudaStream_t s) {
+  using Cfg = WarpChainCfg;
+  auto kern = warp_chain_kernel<NBITS>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(Cfg::SMEM));
+  if (e != cudaSuccess) return e;
+  kern<<<p.n_out * p.slices, Cfg::THREADS, Cfg::SMEM, s>>>(p);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_small_chain(int N, int nbits, bool dual, const ChainParams& p, cudaStream_t s) {
+  // single-pol 1024-point frames: one FFT per warp (warp_chain_kernel)
+  if (N == 1024 && !dual) {
+    switch (nbits) {
+      case 8: return launch_warp_chain_t<8>(p, s);
+      case 10: return launch_warp_chain_t<10>(p, s);
+      case 12: return launch_warp_chain_t<12>(p, s);
+    }
+    return cudaErrorInvalidValue;
+  }
   return dual ? launch_small_d<true>(N, nbits, p, s) : launch_small_d<false>(N, nbits, p, s);
 }
 
@@ -574,7 +790,22 @@ cudaError_t launch_finalize(const ChainParams& p, int npol, int C, int dual, int
   return cudaGetLastError();
 }
 
+// W1024^(lane k1) at [k1 * 32 + lane] (lane, k1 < 32), in FP64 and rounded once.
+__global__ void warp_stage_twiddle_kernel(float2* tw) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 1024) return;
+  const int k1 = i >> 5, lane = i & 31;
+  double sn, cs;
+  sincospi(-2.0 * static_cast<double>(lane * k1) / 1024.0, &sn, &cs);
+  tw[i] = make_float2(static_cast<float>(cs), static_cast<float>(sn));
+}
+
 cudaError_t launch_twiddles(int N, float2* tw, cudaStream_t s) {
+  if (N == 1024) {
+    warp_stage_twiddle_kernel<<<4, 256, 0, s>>>(tw + tw_size(N));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   for (int ns = 1; ns < N; ns *= pass_radix(N, ns)) {
     const int r = pass_radix(N, ns);
     if (ns == 1) continue;

@@ -61,7 +61,10 @@ cudaError_t launch_reduce_finalize(int N, bool dual, const ChainParams& p, int n
                                    float* baselines_out, cudaStream_t s);
 cudaError_t launch_finalize(const ChainParams& p, int npol, int C, int dual, int convention, int ungated,
                             float* baselines_out, cudaStream_t s);
+// Twiddle tables of the shared-memory path: the Stockham tables of N, and
+// at N = 1024 the warp chain's stage table after them (small_tw_size entries).
 cudaError_t launch_twiddles(int N, float2* tw, cudaStream_t s);
+__host__ __device__ constexpr int small_tw_size(int N) { return tw_size(N) + (N == 1024 ? 1024 : 0); }
 cudaError_t launch_fourstep_twiddles(int N, float2* twA, float2* twB, cudaStream_t s);
 cudaError_t launch_gate_debug(int nbits, const GateParams& g, const float* baselines, int npol, uint32_t nsamps,
                               float* out, cudaStream_t s);

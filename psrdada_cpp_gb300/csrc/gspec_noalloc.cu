@@ -108,7 +108,7 @@ extern "C" int gspec_process_block_noalloc(const gspec_config* cfg, const void* 
   const size_t sat_b = align256(h.ext_bytes);
   const size_t masks_b = align256(h.items_per_pol);
   const size_t flags_b = align256(h.batch);
-  const size_t tw_b = align256(static_cast<size_t>(gspec::tw_size(N)) * sizeof(float2));
+  const size_t tw_b = align256(static_cast<size_t>(gspec::small_tw_size(N)) * sizeof(float2));
   const size_t part_b = h.slices > 1 ? align256(h.n_out * h.slices * vals * h.C * sizeof(float)) : 0;
   const size_t need = stats_b + sat_b + masks_b + flags_b + tw_b + part_b;
   if (need > kScratchBytes) {
