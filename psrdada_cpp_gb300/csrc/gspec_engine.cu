@@ -259,6 +259,14 @@ cudaError_t launch_chain(gspec_handle* h, const uint8_t* d_block, uint8_t* d_out
   }
   if (e != cudaSuccess) return e;
   if (h->path == 0) {
+    if (h->d_ticket) {
+      // the chain's last CTA finalises the block (no finalize launch)
+      p.ticket = h->d_ticket;
+      p.fin_baselines = h->d_baselines;
+      p.fin_convention = static_cast<int32_t>(h->cfg.convention);
+      p.fin_ungated = h->ungated ? 1 : 0;
+      return timed(h, 0, s, [&] { return launch_small_chain(N, h->cfg.nbits, h->dual, p, s); });
+    }
     e = timed(h, 0, s, [&] { return launch_small_chain(N, h->cfg.nbits, h->dual, p, s); });
     if (e != cudaSuccess) return e;
     if (h->slices > 1) {
@@ -337,7 +345,7 @@ void release(gspec_handle* h) {
   void* ptrs[] = {h->d_sat_dev, h->d_baselines, h->d_pol_stats, h->d_tw,   h->d_tw1,   h->d_tw2,  h->d_twA,
                   h->d_twB,     h->d_partial,   h->d_scratch,   h->d_masks, h->d_flags, h->d_jobs, h->d_njobs,
                   h->d_dc,      h->d_err,       h->d_tc_parts,  h->d_tc_w,  h->d_tc_img, h->d_bsum,
-                  h->d_dcsum};
+                  h->d_dcsum,   h->d_ticket};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->h_err) cudaFreeHost(h->h_err);
@@ -522,6 +530,12 @@ uint64_t bsum_bytes(const gspec_handle* h) {
   return static_cast<uint64_t>(h->kchunk) * (h->N1 / 2) * (h->dual ? 8 : 2) * (h->N2 + 1) * sizeof(float);
 }
 
+// The warp chain finalises the block in its last CTA when each CTA holds
+// whole spectra (no partial sums to reduce first).
+bool fused_finalize(const gspec_handle* h) {
+  return h->path == 0 && h->slices == 1 && uses_warp_chain(static_cast<int>(h->cfg.fft_length), h->dual);
+}
+
 // Device bytes gspec_create allocates for a planned handle (the same list
 // and the same 16-byte minimum as its dalloc calls).
 uint64_t footprint(const gspec_handle* h) {
@@ -534,6 +548,7 @@ uint64_t footprint(const gspec_handle* h) {
   if (h->path == 0) {
     t += sz(small_tw_size(static_cast<int>(N)) * sizeof(float2));
     if (h->slices > 1) t += sz(h->n_out * h->slices * vals * h->C * sizeof(float));
+    if (fused_finalize(h)) t += sz(sizeof(uint32_t));
   } else {
     t += sz(tw_size(static_cast<int>(h->N1)) * sizeof(float2)) + sz(tw_size(static_cast<int>(h->N2)) * sizeof(float2));
     t += 2 * sz(1024 * sizeof(float2));
@@ -647,6 +662,10 @@ gspec_handle* gspec_create(const gspec_config* cfg, char* err, size_t err_len) {
     if (h->slices > 1 &&
         !dalloc(h, &h->d_partial, h->n_out * h->slices * vals * h->C * sizeof(float), "partials"))
       return bail("");
+    if (gspec_engine::fused_finalize(h)) {
+      if (!dalloc(h, &h->d_ticket, sizeof(uint32_t), "chain ticket")) return bail("");
+      cudaMemset(h->d_ticket, 0, sizeof(uint32_t));
+    }
   } else {
     if (!dalloc(h, &h->d_tw1, tw_size(h->N1) * sizeof(float2), "twiddles") ||
         !dalloc(h, &h->d_tw2, tw_size(h->N2) * sizeof(float2), "twiddles") ||

@@ -58,6 +58,7 @@ struct gspec_handle {
   uint32_t maxjobs = 0;
   int32_t heap_shift = -1;
   uint32_t* d_err = nullptr;       // set by kernels whose bounded waits gave up
+  uint32_t* d_ticket = nullptr;    // warp chain with whole spectra per CTA: CTAs done (its last one finalises)
   uint32_t* h_err = nullptr;       // pinned copy, refreshed after every block
   uint32_t* h_err_dev = nullptr;   // its device address (written by the block's finalisation)
   cudaStream_t h2d = nullptr, proc = nullptr, d2h = nullptr;
@@ -87,6 +88,8 @@ bool configure_handle(gspec_handle* h);
 bool plan_units(gspec_handle* h);
 // SM count, work units / scratch chunk (after configure_handle).
 bool plan_handle(gspec_handle* h);
+// The chain's last CTA finalises the block (warp chain, whole spectra per CTA).
+bool fused_finalize(const gspec_handle* h);
 // Device bytes gspec_create allocates for a planned handle.
 uint64_t footprint(const gspec_handle* h);
 uint64_t bsum_bytes(const gspec_handle* h);

@@ -292,6 +292,11 @@ __global__ void __launch_bounds__(SmallCfg<N, DUAL>::THREADS, GSPEC_SMALL_MINB)
   commit_stats<NPOL>(p, st, k, Cfg::VALS * C, red);
 }
 
+// Block finalisation (counters, baselines of the next block, error-word
+// mirror); `red` holds 2 x (warps of the CTA) 64-bit words of shared memory.
+__device__ void finalize_block(const ChainParams& p, int npol, int C, int dual, int convention, int ungated,
+                               float* baselines_out, unsigned long long* red);
+
 // ------------------------------------------------------------ warp chain
 // Single-pol 1024-point chain with one FFT per warp (N = 32 x 32).  Lane l
 // unpacks and gates the 32 consecutive samples 32 l .. 32 l + 31 of each of
@@ -487,6 +492,18 @@ __global__ void __launch_bounds__(WarpChainCfg::THREADS, 2) warp_chain_kernel(Ch
   }
   GateStats sts[1] = {st};
   commit_stats<1>(p, sts, k, 2 * C, red);
+  if (p.ticket) {
+    // the last CTA to finish runs the block finalisation: every CTA makes its
+    // outputs and counters visible device-wide before it takes its ticket
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) jinfo[3] = atomicInc(p.ticket, gridDim.x - 1) == gridDim.x - 1 ? 1u : 0u;
+    __syncthreads();
+    if (jinfo[3]) {
+      __threadfence();
+      finalize_block(p, 1, C, 0, p.fin_convention, p.fin_ungated, p.fin_baselines, red);
+    }
+  }
 }
 
 // Pre-pass of a block: the gate masks of every side-channel item index of
@@ -531,8 +548,7 @@ __global__ void gate_prepass_kernel(GateParams g, uint32_t nitems, uint8_t* mask
 // and the device error word into its page-locked host mirror.  Run by every
 // thread of one CTA after every counter of the block is final.
 __device__ void finalize_block(const ChainParams& p, int npol, int C, int dual, int convention, int ungated,
-                               float* baselines_out) {
-  __shared__ unsigned long long red[2 * 32];
+                               float* baselines_out, unsigned long long* red) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nwarps = (blockDim.x + 31) >> 5;
   const int vals = dual ? 8 : 2;
@@ -595,7 +611,8 @@ __device__ void finalize_block(const ChainParams& p, int npol, int C, int dual, 
 
 __global__ void finalize_kernel(ChainParams p, int npol, int C, int dual, int convention, int ungated,
                                 float* baselines_out) {
-  finalize_block(p, npol, C, dual, convention, ungated, baselines_out);
+  __shared__ unsigned long long red[2 * 32];
+  finalize_block(p, npol, C, dual, convention, ungated, baselines_out, red);
 }
 
 // out[k][i] += sum_s partial[k][s][i] (fixed order); the last block of the
@@ -610,8 +627,9 @@ __global__ void reduce_finalize_kernel(ChainParams p, int vals_c, int npol, int 
     for (uint32_t s = 0; s < p.slices; ++s) v += src[static_cast<size_t>(s) * vals_c];
     outf[i] = p.store ? v : outf[i] + v;
   }
+  __shared__ unsigned long long red[2 * 32];
   if (blockIdx.x == gridDim.x - 1 && blockIdx.y == gridDim.y - 1)
-    finalize_block(p, npol, C, dual, convention, ungated, baselines_out);
+    finalize_block(p, npol, C, dual, convention, ungated, baselines_out, red);
 }
 
 // --------------------------------------------------------------- twiddles
@@ -752,7 +770,7 @@ static cudaError_t launch_warp_chain_t(const ChainParams& p, cudaStream_t s) {
 
 cudaError_t launch_small_chain(int N, int nbits, bool dual, const ChainParams& p, cudaStream_t s) {
   // single-pol 1024-point frames: one FFT per warp (warp_chain_kernel)
-  if (N == 1024 && !dual) {
+  if (uses_warp_chain(N, dual)) {
     switch (nbits) {
       case 8: return launch_warp_chain_t<8>(p, s);
       case 10: return launch_warp_chain_t<10>(p, s);

@@ -32,6 +32,10 @@ struct ChainParams {
   volatile uint32_t* err_host;     // page-locked mirror of *dev_err written by the finalisation (or null)
   uint32_t store;                  // 1: one block per output, so each launch writes every spectrum value of
                                    // its records (stores, no read-add); only the counters start from zero
+  // finalisation by the chain's last CTA instead of a finalize launch (warp chain; ticket null: off)
+  uint32_t* ticket;                // CTAs done with the block, modulo the grid size (zero between launches)
+  float* fin_baselines;            // the block finalisation's baselines_out
+  int32_t fin_convention, fin_ungated;
 };
 
 // Large-N (four-step) parameters.
@@ -56,6 +60,8 @@ struct FourStepParams {
 };
 
 // Host-side launchers (gspec_kernels.cu).
+// Shared-memory path shapes run by the warp chain (one FFT per warp): single-pol 1024-point frames.
+constexpr bool uses_warp_chain(int N, bool dual) { return N == 1024 && !dual; }
 cudaError_t launch_small_chain(int N, int nbits, bool dual, const ChainParams& p, cudaStream_t s);
 cudaError_t launch_reduce_finalize(int N, bool dual, const ChainParams& p, int npol, int convention, int ungated,
                                    float* baselines_out, cudaStream_t s);
