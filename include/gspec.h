@@ -164,7 +164,8 @@ int gspec_run_block_device(gspec_handle* h, const void* d_block, void* d_out, vo
  * zeroes its accumulators with thrust::fill, edd/detail/GatedSpectrometer.cu):
  * when each block holds whole outputs (gspec_info.n_blocks == 1) every
  * spectrum value is stored by the block, so only each record's counters are
- * zeroed; otherwise the whole buffer. */
+ * zeroed (nothing, where the block stores the counters too: single-pol
+ * 1024-point spectra with one CTA per spectrum); otherwise the whole buffer. */
 int gspec_clear_output_device(gspec_handle* h, void* d_out, void* cuda_stream);
 
 int gspec_get_info(const gspec_handle* h, gspec_info* info);

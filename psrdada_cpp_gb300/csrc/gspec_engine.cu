@@ -460,6 +460,8 @@ namespace gspec_engine {
 // block (ChainParams::store), so only each record's counters (added to by
 // the block's atomics); otherwise the whole buffer.
 cudaError_t clear_output(const gspec_handle* h, uint8_t* d_out, cudaStream_t s) {
+  // the warp chain with whole spectra per CTA stores the counters as well
+  if (h->n_blocks == 1 && path0_stores_records(h)) return cudaSuccess;
   if (h->n_blocks == 1) {
     const uint64_t spectra = (h->dual ? 8 : 2) * h->C * 4;
     return cudaMemset2DAsync(d_out + spectra, h->rec, 0, h->rec - spectra, h->n_out, s);
@@ -535,6 +537,10 @@ uint64_t bsum_bytes(const gspec_handle* h) {
 bool fused_finalize(const gspec_handle* h) {
   return h->path == 0 && h->slices == 1 && uses_warp_chain(static_cast<int>(h->cfg.fft_length), h->dual);
 }
+
+// With one block per output, the same chain stores every word of each
+// record (spectra and counters), so the output needs no clearing.
+bool path0_stores_records(const gspec_handle* h) { return fused_finalize(h); }
 
 // Device bytes gspec_create allocates for a planned handle (the same list
 // and the same 16-byte minimum as its dalloc calls).

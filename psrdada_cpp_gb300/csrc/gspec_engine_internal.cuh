@@ -90,6 +90,8 @@ bool plan_units(gspec_handle* h);
 bool plan_handle(gspec_handle* h);
 // The chain's last CTA finalises the block (warp chain, whole spectra per CTA).
 bool fused_finalize(const gspec_handle* h);
+// One block per output then writes every word of its records (no clearing).
+bool path0_stores_records(const gspec_handle* h);
 // Device bytes gspec_create allocates for a planned handle.
 uint64_t footprint(const gspec_handle* h);
 uint64_t bsum_bytes(const gspec_handle* h);

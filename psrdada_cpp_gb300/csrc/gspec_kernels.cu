@@ -22,6 +22,11 @@
 #define GSPEC_SMALL_TW_SMEM 0
 #endif
 
+// Programmatic dependent launch of the warp chain after the gate pre-pass.
+#ifndef GSPEC_PDL
+#define GSPEC_PDL 1
+#endif
+
 namespace gspec {
 
 // ------------------------------------------------------------------ helpers
@@ -57,7 +62,7 @@ __device__ __forceinline__ bool block_sum_u64(unsigned long long (&vals)[NV], un
 //   record counters of spectrum k; sat0, sat1 -> sat[k].
 template <int NPOL>
 __device__ __forceinline__ void commit_stats(const ChainParams& p, const GateStats (&st)[NPOL], uint32_t k,
-                                             int vals_c, unsigned long long* red) {
+                                             int vals_c, unsigned long long* red, bool store_counts = false) {
   constexpr int NV = 4 * NPOL + 4;
   unsigned long long v[NV];
 #pragma unroll
@@ -89,7 +94,13 @@ __device__ __forceinline__ void commit_stats(const ChainParams& p, const GateSta
       if (j < 2) {
         unsigned long long* cnt =
             reinterpret_cast<unsigned long long*>(p.out + k * p.out_rec + static_cast<uint64_t>(vals_c) * 4);
-        if (tot) atomicAdd(cnt + j, tot);
+        // store_counts: this CTA holds all of spectrum k's frames of an output
+        // that one block fills, so its counts are the record's counters
+        if (store_counts) {
+          cnt[j] = tot;
+        } else if (tot) {
+          atomicAdd(cnt + j, tot);
+        }
       } else {
         if (tot) atomicAdd(p.sat + 2 * k + (j - 2), tot);
       }
@@ -383,14 +394,19 @@ __global__ void __launch_bounds__(WarpChainCfg::THREADS, 2) warp_chain_kernel(Ch
   const uint32_t k = unit / p.slices;
   const uint32_t sl = unit - k * p.slices;
   const uint32_t f0 = k * p.nacc + sl * p.frames_per_unit;
+  // the stage twiddles W1024^(lane k1) follow the Stockham tables of N
+  for (int i = tid; i < 1024; i += Cfg::THREADS) tw[i] = __ldg(p.tw + tw_size(N) + i);
+#if GSPEC_PDL
+  // launched as a programmatic dependent of the gate pre-pass: its masks and
+  // frame flags are complete once this returns
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
   if (tid == 0) {
     uint32_t dc[2];
     jinfo[0] = build_jobs(p.flags + f0, p.frames_per_unit, false, jobs, dc);
     jinfo[1] = dc[0];
     jinfo[2] = dc[1];
   }
-  // the stage twiddles W1024^(lane k1) follow the Stockham tables of N
-  for (int i = tid; i < 1024; i += Cfg::THREADS) tw[i] = __ldg(p.tw + tw_size(N) + i);
   const float b0 = p.baselines[0], b1 = p.baselines[1];
   __syncthreads();
   const uint32_t njobs = jinfo[0];
@@ -491,7 +507,7 @@ __global__ void __launch_bounds__(WarpChainCfg::THREADS, 2) warp_chain_kernel(Ch
     }
   }
   GateStats sts[1] = {st};
-  commit_stats<1>(p, sts, k, 2 * C, red);
+  commit_stats<1>(p, sts, k, 2 * C, red, p.store && p.slices == 1);
   if (p.ticket) {
     // the last CTA to finish runs the block finalisation: every CTA makes its
     // outputs and counters visible device-wide before it takes its ticket
@@ -513,6 +529,11 @@ __global__ void __launch_bounds__(WarpChainCfg::THREADS, 2) warp_chain_kernel(Ch
 // monotonic inside a gating chunk and frames never straddle chunks).
 __global__ void gate_prepass_kernel(GateParams g, uint32_t nitems, uint8_t* masks, uint32_t N, uint32_t nframes,
                                     uint8_t* flags, uint32_t L) {
+#if GSPEC_PDL
+  // a programmatic dependent (the warp chain) may start its prologue now; it
+  // waits for this grid's completion before it reads masks or flags
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nitems; i += stride) {
     bool m0, m1;
@@ -764,8 +785,22 @@ static cudaError_t launch_warp_chain_t(const ChainParams& p, cudaStream_t s) {
   auto kern = warp_chain_kernel<NBITS>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(Cfg::SMEM));
   if (e != cudaSuccess) return e;
+#if GSPEC_PDL
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(p.n_out * p.slices);
+  cfg.blockDim = dim3(Cfg::THREADS);
+  cfg.dynamicSmemBytes = Cfg::SMEM;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, p);
+#else
   kern<<<p.n_out * p.slices, Cfg::THREADS, Cfg::SMEM, s>>>(p);
   return cudaGetLastError();
+#endif
 }
 
 cudaError_t launch_small_chain(int N, int nbits, bool dual, const ChainParams& p, cudaStream_t s) {

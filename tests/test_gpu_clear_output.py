@@ -1,7 +1,8 @@
 """gspec_clear_output_device: with one block per output the chain stores every
 spectrum value, so clearing only the counters of a buffer that holds garbage
-gives the same bytes as a fully zeroed buffer; with several blocks per output
-the whole buffer is cleared.  Shared-memory and four-step paths, single and
+(or nothing, where the chain stores the counters as well) gives the same bytes
+as a fully zeroed buffer; with several blocks per output the whole buffer is
+cleared.  Shared-memory and four-step paths, single and
 dual pol, FP32 and the tensor-core form."""
 import numpy as np
 import pytest
@@ -15,6 +16,8 @@ torch = pytest.importorskip("torch")
 CASES = [
     # (spec, form): n_blocks = 1 unless the block holds less than fft * naccumulate
     (synth.StreamSpec("s8_small", 8, False, 4096, 1, 1 << 18, 1024, 64, diode_period_heaps=3), G.FORM_FP32),
+    # 256 spectra: one warp-chain CTA per spectrum stores its counters too (clearing is a no-op)
+    (synth.StreamSpec("s8_whole", 8, False, 4096, 1, 1 << 24, 1024, 64, diode_period_heaps=3), G.FORM_FP32),
     (synth.StreamSpec("d12_small_slices", 12, True, 6144, 1, 1 << 16, 2048, 8, diode_period_heaps=2), G.FORM_FP32),
     (synth.StreamSpec("d12_fs", 12, True, 6144, 1, 1 << 18, 1 << 16, 4, diode_period_heaps=2), G.FORM_FP32),
     (synth.StreamSpec("d12_fs_bf16", 12, True, 6144, 1, 1 << 18, 1 << 16, 4, diode_period_heaps=2), G.FORM_BF16),
