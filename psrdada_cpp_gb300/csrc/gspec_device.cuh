@@ -346,6 +346,9 @@ __device__ __forceinline__ void unpack_group(const uint8_t* __restrict__ p, int 
 
 // Unpack S samples that start on a 4-byte boundary (S * NBITS a multiple of
 // 32 bits): the part of a group that a tile narrower than the group keeps.
+#ifndef GSPEC_SPAN_WIDE
+#define GSPEC_SPAN_WIDE 1
+#endif
 template <int NBITS, int S>
 __device__ __forceinline__ void unpack_span(const uint8_t* __restrict__ p, int (&out)[S]) {
   if constexpr (S == Group<NBITS>::samples) {
@@ -355,8 +358,24 @@ __device__ __forceinline__ void unpack_span(const uint8_t* __restrict__ p, int (
     constexpr int NW = S * NBITS / 32;
     uint32_t W[NW + 1];
     const uint32_t* q = reinterpret_cast<const uint32_t*>(p);
+    if constexpr (NW == 3 && GSPEC_SPAN_WIDE) {
+      // three words as one 8-byte and one 4-byte load (the 8-byte one on
+      // whichever side of p is 8-byte aligned): two requests instead of three
+      if (reinterpret_cast<uintptr_t>(p) & 7u) {
+        const uint2 t = __ldg(reinterpret_cast<const uint2*>(q + 1));
+        W[0] = bswap32(__ldg(q));
+        W[1] = bswap32(t.x);
+        W[2] = bswap32(t.y);
+      } else {
+        const uint2 t = __ldg(reinterpret_cast<const uint2*>(q));
+        W[0] = bswap32(t.x);
+        W[1] = bswap32(t.y);
+        W[2] = bswap32(__ldg(q + 2));
+      }
+    } else {
 #pragma unroll
-    for (int w = 0; w < NW; ++w) W[w] = bswap32(__ldg(q + w));
+      for (int w = 0; w < NW; ++w) W[w] = bswap32(__ldg(q + w));
+    }
     W[NW] = 0;
 #pragma unroll
     for (int i = 0; i < S; ++i) {
