@@ -349,8 +349,10 @@ __device__ __forceinline__ void unpack_group(const uint8_t* __restrict__ p, int 
 #ifndef GSPEC_SPAN_WIDE
 #define GSPEC_SPAN_WIDE 1
 #endif
+// win16: p lies in a buffer made of whole 16-byte chunks, so the aligned
+// 16-byte chunk around the span may be read whole.
 template <int NBITS, int S>
-__device__ __forceinline__ void unpack_span(const uint8_t* __restrict__ p, int (&out)[S]) {
+__device__ __forceinline__ void unpack_span(const uint8_t* __restrict__ p, int (&out)[S], bool win16 = false) {
   if constexpr (S == Group<NBITS>::samples) {
     unpack_group<NBITS>(p, out);
   } else {
@@ -359,9 +361,16 @@ __device__ __forceinline__ void unpack_span(const uint8_t* __restrict__ p, int (
     uint32_t W[NW + 1];
     const uint32_t* q = reinterpret_cast<const uint32_t*>(p);
     if constexpr (NW == 3 && GSPEC_SPAN_WIDE) {
-      // three words as one 8-byte and one 4-byte load (the 8-byte one on
-      // whichever side of p is 8-byte aligned): two requests instead of three
-      if (reinterpret_cast<uintptr_t>(p) & 7u) {
+      // three words: one 16-byte load when they lie in one aligned 16-byte
+      // chunk of a whole-chunk buffer, else one 8-byte and one 4-byte load
+      // (the 8-byte one on whichever side of p is 8-byte aligned)
+      const uint32_t mis = static_cast<uint32_t>(reinterpret_cast<uintptr_t>(p) & 15u);
+      if (win16 && mis <= 4u) {
+        const uint4 t = __ldg(reinterpret_cast<const uint4*>(p - mis));
+        W[0] = bswap32(mis ? t.y : t.x);
+        W[1] = bswap32(mis ? t.z : t.y);
+        W[2] = bswap32(mis ? t.w : t.z);
+      } else if (mis & 4u) {
         const uint2 t = __ldg(reinterpret_cast<const uint2*>(q + 1));
         W[0] = bswap32(__ldg(q));
         W[1] = bswap32(t.x);
@@ -414,6 +423,7 @@ struct GateParams {
   int32_t heap_shift;        // intended convention: log2(samples per heap) when that is an integer power of 2, else -1
   const uint8_t* masks;      // per item index: bit0 = gate 0 (m0), bit1 = gate 1 (m1); built by the mask pass
   uint64_t heap_magic;       // ceil(2^64 / heap_size), 0 for heap_size 1 (see heap_of)
+  uint32_t win16;            // 1: the block is 16-byte aligned and a whole number of 16-byte chunks long
 };
 
 // n / heap_size for 32-bit n without a division: with M = ceil(2^64 / d) =
@@ -503,7 +513,7 @@ __device__ __forceinline__ void gate_group(const GateParams& g, int pol, uint32_
                                            DcAcc* dc1 = nullptr) {
   int v[GS];
   const uint64_t byte0 = static_cast<uint64_t>(s) * NBITS / 8;
-  unpack_span<NBITS, GS>(pol_byte(g, pol, byte0), v);
+  unpack_span<NBITS, GS>(pol_byte(g, pol, byte0), v, g.win16 != 0);
   const uint32_t ia = item_index(g, s);
   const uint32_t ib = item_index(g, s + GS - 1);
   bool a0, a1;
@@ -592,7 +602,7 @@ __device__ __forceinline__ void gate_group1(const GateParams& g, int pol, uint32
                                             float (&out)[GS], GateStats& st, bool stats, DcAcc* dc = nullptr) {
   int v[GS];
   const uint64_t byte0 = static_cast<uint64_t>(s) * NBITS / 8;
-  unpack_span<NBITS, GS>(pol_byte(g, pol, byte0), v);
+  unpack_span<NBITS, GS>(pol_byte(g, pol, byte0), v, g.win16 != 0);
   const uint32_t ia = item_index(g, s);
   const uint32_t ib = item_index(g, s + GS - 1);
   const uint32_t sh = gate ? 1u : 0u;
@@ -656,8 +666,8 @@ __device__ __forceinline__ void gate_group_dual(const GateParams& g, uint32_t s,
   const uint32_t h = heap_of(g, byte0);
   const uint8_t* p0 = g.block + 2ull * h * g.heap_size + (byte0 - h * g.heap_size);
   int v0[GS], v1[GS];
-  unpack_span<NBITS, GS>(p0, v0);
-  unpack_span<NBITS, GS>(p0 + g.heap_size, v1);
+  unpack_span<NBITS, GS>(p0, v0, g.win16 != 0);
+  unpack_span<NBITS, GS>(p0 + g.heap_size, v1, g.win16 != 0);
   const uint32_t ia = item_index(g, s);
   const uint32_t ib = item_index(g, s + GS - 1);
   const uint32_t sh = gate ? 1u : 0u;

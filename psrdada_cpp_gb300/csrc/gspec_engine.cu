@@ -192,6 +192,7 @@ GateParams gate_params(const gspec_handle* h, const uint8_t* block) {
   g.nbits = h->cfg.nbits;
   g.heap_shift = h->heap_shift;
   g.masks = h->d_masks;
+  g.win16 = (h->cfg.buffer_size % 16 == 0 && reinterpret_cast<uintptr_t>(block) % 16 == 0) ? 1u : 0u;
   return g;
 }
 
