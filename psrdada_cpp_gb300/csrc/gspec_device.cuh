@@ -320,16 +320,47 @@ __device__ __forceinline__ uint32_t bswap32(uint32_t x) { return __byte_perm(x, 
 // Unpack one group from `p` (8-byte aligned, global memory) into out[]
 // as signed integers.  The 64-bit words are read as little-endian 32-bit
 // halves and byte-swapped into a big-endian bit stream W[0..2*words).
+// 12-bit groups (three words) are read as one 16-byte load on the 16-byte
+// aligned side and one 8-byte load.
+#ifndef GSPEC_GROUP_WIDE
+#define GSPEC_GROUP_WIDE 1
+#endif
 template <int NBITS>
 __device__ __forceinline__ void unpack_group(const uint8_t* __restrict__ p, int (&out)[Group<NBITS>::samples]) {
-  constexpr int NW = 2 * Group<NBITS>::words;
+  constexpr int NG = Group<NBITS>::words;
+  constexpr int NW = 2 * NG;
   uint32_t W[NW + 1];
   const uint2* q = reinterpret_cast<const uint2*>(p);
+  uint2 u[NG];
+  if constexpr (NG != 3 || !GSPEC_GROUP_WIDE) {
+    // one word (8 bit); five (10 bit) stay 8-byte loads: the 16-byte form
+    // costs the 10-bit column pass registers
 #pragma unroll
-  for (int w = 0; w < Group<NBITS>::words; ++w) {
-    uint2 u = __ldg(q + w);
-    W[2 * w] = bswap32(u.x);
-    W[2 * w + 1] = bswap32(u.y);
+    for (int w = 0; w < NG; ++w) u[w] = __ldg(q + w);
+  } else if (reinterpret_cast<uintptr_t>(p) & 8u) {
+    // one word before the 16-byte boundary, then pairs
+    u[0] = __ldg(q);
+#pragma unroll
+    for (int a = 1; a + 1 < NG; a += 2) {
+      const uint4 t = __ldg(reinterpret_cast<const uint4*>(q + a));
+      u[a] = make_uint2(t.x, t.y);
+      u[a + 1] = make_uint2(t.z, t.w);
+    }
+    if constexpr ((NG & 1) == 0) u[NG - 1] = __ldg(q + NG - 1);
+  } else {
+    // pairs from p on, then a last word when NG is odd
+#pragma unroll
+    for (int a = 0; a + 1 < NG; a += 2) {
+      const uint4 t = __ldg(reinterpret_cast<const uint4*>(q + a));
+      u[a] = make_uint2(t.x, t.y);
+      u[a + 1] = make_uint2(t.z, t.w);
+    }
+    if constexpr (NG & 1) u[NG - 1] = __ldg(q + NG - 1);
+  }
+#pragma unroll
+  for (int w = 0; w < NG; ++w) {
+    W[2 * w] = bswap32(u[w].x);
+    W[2 * w + 1] = bswap32(u[w].y);
   }
   W[NW] = 0;
 #pragma unroll
@@ -380,6 +411,20 @@ __device__ __forceinline__ void unpack_span(const uint8_t* __restrict__ p, int (
         W[0] = bswap32(t.x);
         W[1] = bswap32(t.y);
         W[2] = bswap32(__ldg(q + 2));
+      }
+    } else if constexpr (NW % 4 == 0) {
+      if ((reinterpret_cast<uintptr_t>(p) & 15u) == 0) {
+#pragma unroll
+        for (int w = 0; w < NW; w += 4) {
+          const uint4 t = __ldg(reinterpret_cast<const uint4*>(q + w));
+          W[w] = bswap32(t.x);
+          W[w + 1] = bswap32(t.y);
+          W[w + 2] = bswap32(t.z);
+          W[w + 3] = bswap32(t.w);
+        }
+      } else {
+#pragma unroll
+        for (int w = 0; w < NW; ++w) W[w] = bswap32(__ldg(q + w));
       }
     } else {
 #pragma unroll
