@@ -640,14 +640,45 @@ __device__ __forceinline__ void gate_group(const GateParams& g, int pol, uint32_
   }
 }
 
+#ifndef GSPEC_SIMD8
+#define GSPEC_SIMD8 1
+#endif
+
 // One gate of one group: out[] = gate `gate` of the samples; statistics of
-// that gate only when `stats` is set.
+// that gate only when `stats` is set.  8-bit spans of whole 16-byte chunks
+// keep the raw words: a sample is the sign-extended byte at its address, and
+// a span inside one item sums its samples four at a time (dp4a against
+// 0x01010101) and counts its saturated ones by byte compares (-128 = 0x80,
+// 127 = 0x7f) and a population count.
 template <int NBITS, int GS = Group<NBITS>::samples>
 __device__ __forceinline__ void gate_group1(const GateParams& g, int pol, uint32_t s, float b, int gate,
                                             float (&out)[GS], GateStats& st, bool stats, DcAcc* dc = nullptr) {
+  constexpr bool kSimd8 = GSPEC_SIMD8 && NBITS == 8 && GS % 16 == 0;
   int v[GS];
   const uint64_t byte0 = static_cast<uint64_t>(s) * NBITS / 8;
-  unpack_span<NBITS, GS>(pol_byte(g, pol, byte0), v, g.win16 != 0);
+  [[maybe_unused]] uint32_t raw[kSimd8 ? GS / 4 : 1];
+  if constexpr (kSimd8) {
+    // the span starts on a 4-byte boundary (GS samples of whole words)
+    const uint8_t* p = pol_byte(g, pol, byte0);
+    const uint32_t* q = reinterpret_cast<const uint32_t*>(p);
+    if ((reinterpret_cast<uintptr_t>(p) & 15u) == 0) {
+#pragma unroll
+      for (int w = 0; w < GS / 4; w += 4) {
+        const uint4 t = __ldg(reinterpret_cast<const uint4*>(q + w));
+        raw[w] = t.x;
+        raw[w + 1] = t.y;
+        raw[w + 2] = t.z;
+        raw[w + 3] = t.w;
+      }
+    } else {
+#pragma unroll
+      for (int w = 0; w < GS / 4; ++w) raw[w] = __ldg(q + w);
+    }
+#pragma unroll
+    for (int i = 0; i < GS; ++i) v[i] = static_cast<int>(static_cast<int8_t>(raw[i >> 2] >> (8 * (i & 3))));
+  } else {
+    unpack_span<NBITS, GS>(pol_byte(g, pol, byte0), v, g.win16 != 0);
+  }
   const uint32_t ia = item_index(g, s);
   const uint32_t ib = item_index(g, s + GS - 1);
   const uint32_t sh = gate ? 1u : 0u;
@@ -661,8 +692,19 @@ __device__ __forceinline__ void gate_group1(const GateParams& g, int pol, uint32
       const float vf = static_cast<float>(v[i]);
       out[i] = gate_value(vf, b, ma);
       if (dc) res += out[i] - vf;
-      sumv += v[i];
-      satc += (v[i] == lo) | (v[i] == hi);
+      if constexpr (!kSimd8) {
+        sumv += v[i];
+        satc += (v[i] == lo) | (v[i] == hi);
+      }
+    }
+    if constexpr (kSimd8) {
+      uint32_t satbits = 0;
+#pragma unroll
+      for (int w = 0; w < GS / 4; ++w) {
+        sumv = __dp4a(static_cast<int>(raw[w]), 0x01010101, sumv);
+        satbits += __popc(__vcmpeq4(raw[w], 0x80808080u) | __vcmpeq4(raw[w], 0x7f7f7f7fu));
+      }
+      satc = static_cast<int>(satbits >> 3);
     }
     cnt = ma ? GS : 0;
     if (!ma) sumv = satc = 0;
