@@ -498,6 +498,9 @@ def measure_form(args, form_name, spec, kind, host_blocks, d_blocks, dev, clocks
     in_bytes = spec.buffer_size
     out_bytes = int(info.output_bytes)
     launches_per_block = {k: v[1] / nprof for k, v in kernels.items()}
+    # engine stage names: "small_chain" is the shared-memory path's chain launch
+    # (warp_chain_kernel for single-pol 1024-point frames), reading the block and
+    # writing the records
     if dom in ("fourstep_a", "small_chain"):
         alg_bytes_launch = (in_bytes + (out_bytes if dom == "small_chain" else 0)) / launches_per_block[dom]
     elif dom == "fourstep_b":
